@@ -1,0 +1,221 @@
+"""aether_gb300: GB300-native fused batched-expression engine.
+
+Python host mirror of the reference's consumer surface for the fused
+assignment path. Arrays are SoA (component planes at a pitch of the capacity,
+a multiple of 32 samples: array/Array.h:80,288-304); expressions are built
+lazily (expr.py) and `assign(dst, expr)` evaluates `dst[i] = expr` for every
+sample in one sm_103a kernel generated from the tree and cached by its hash.
+
+Device memory and streams come from PyTorch; every kernel comes from
+libaether_gb300.so. There is no CPU evaluation path in this package.
+"""
+
+import ctypes
+import threading
+
+from . import _abi
+from ._abi import AetherError, lowering
+from .expr import (Expr, Generator, IrContext, Operand, Scalar, clamp, constant, cwiseAbs, cwiseAcos, cwiseAsin,
+                   cwiseAtan, cwiseCos, cwiseDiv, cwiseExp, cwiseExpm1, cwiseLog, cwiseLog1p, cwiseMax, cwiseMin,
+                   cwisePow, cwiseRsqrt, cwiseSign, cwiseSin, cwiseSqrt, cwiseSquare, cwiseTan, cwiseTanh, literal,
+                   plan_text, select, splitmix64, stack)
+
+CAPACITY_ALIGNMENT = 32
+_DTYPES = {"f64": 8, "f32": 4}
+
+
+def quantized_capacity(n):
+    """Array capacity: n rounded up to a multiple of 32 samples (array/Array.h:80, :288-295)."""
+    return max(CAPACITY_ALIGNMENT, (int(n) + CAPACITY_ALIGNMENT - 1) // CAPACITY_ALIGNMENT * CAPACITY_ALIGNMENT)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _tdtype(dtype):
+    torch = _torch()
+    return {"f64": torch.float64, "f32": torch.float32}[dtype]
+
+
+class Array:
+    """Owning SoA array on the GPU: `shape` components x `n` samples.
+
+    `data` is a torch tensor (components, capacity); plane c starts at
+    c * capacity elements, 256-byte aligned for both f64 and f32."""
+
+    def __init__(self, dtype, shape, n, device="cuda", data=None):
+        if isinstance(shape, int):
+            shape = (shape,)
+        self.dtype = dtype
+        self.shape = tuple(shape)
+        self.comps = 1
+        for s in self.shape:
+            self.comps *= s
+        self.n = int(n)
+        if data is not None:
+            self.data = data
+            self.capacity = data.shape[1]
+        else:
+            self.capacity = quantized_capacity(n)
+            self.data = _torch().zeros((self.comps, self.capacity), dtype=_tdtype(dtype), device=device)
+
+    @classmethod
+    def wrap(cls, tensor, shape=None, n=None):
+        """View a (components, pitch) tensor as an array without copying."""
+        dtype = {"torch.float64": "f64", "torch.float32": "f32"}[str(tensor.dtype)]
+        shape = shape or (tensor.shape[0],)
+        return cls(dtype, shape, n if n is not None else tensor.shape[1], data=tensor)
+
+    def samples(self):
+        return self.n
+
+    def view(self):
+        """The array as an expression leaf (deviceView() of the reference)."""
+        return Operand(self.data.data_ptr(), self.capacity, self.dtype, self.shape, owner=self)
+
+    __call__ = view
+
+    def host(self):
+        return self.data[:, : self.n].cpu().numpy()
+
+    def upload(self, host):
+        torch = _torch()
+        t = torch.as_tensor(host).to(self.data.dtype)
+        self.data[:, : self.n].copy_(t.reshape(self.comps, self.n))
+        return self
+
+
+class Plan:
+    """A compiled plan: one aether-ir/1 text, one kernel."""
+
+    def __init__(self, ir, low=None):
+        self.ir = ir
+        self.low = low
+        h = ctypes.c_void_p()
+        _abi.check(_abi.lib().aether_plan_create(ir.encode(), ctypes.byref(low) if low else None, ctypes.byref(h)))
+        self.handle = h
+
+    def info(self):
+        i = _abi.AetherPlanInfo()
+        _abi.check(_abi.lib().aether_plan_info(self.handle, ctypes.byref(i)))
+        return i
+
+    def source(self):
+        n = ctypes.c_size_t()
+        _abi.check(_abi.lib().aether_plan_source(self.handle, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value + 1)
+        _abi.check(_abi.lib().aether_plan_source(self.handle, buf, n.value + 1, ctypes.byref(n)))
+        return buf.value.decode()
+
+    def workspace_size(self, n):
+        b = ctypes.c_uint64()
+        _abi.check(_abi.lib().aether_plan_workspace_size(self.handle, n, ctypes.byref(b)))
+        return b.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _abi.lib().aether_plan_release(self.handle)
+        except Exception:
+            pass
+
+
+_cache = {}
+_cache_lock = threading.Lock()
+
+
+def get_plan(ir, block=0, ipt=0, vec=0, contract=-1, math=0, min_blocks=0):
+    key = (ir, block, ipt, vec, contract, math, min_blocks)
+    with _cache_lock:
+        p = _cache.get(key)
+    if p is None:
+        p = Plan(ir, lowering(block, ipt, vec, contract, math, min_blocks))
+        with _cache_lock:
+            _cache[key] = p
+    return p
+
+
+class Launch:
+    """A plan bound to its arguments: re-launchable without rebuilding the IR."""
+
+    def __init__(self, plan, ctx, n, dst_ptr, dst_pitch, sample_offset=0, reduce_ptr=None, workspace=None):
+        self.plan = plan
+        self._ops = (_abi.AetherOperand * max(1, len(ctx.operands)))()
+        for i, (ptr, pitch, _dt, _c, _owner) in enumerate(ctx.operands):
+            self._ops[i].ptr = ptr
+            self._ops[i].pitch = pitch
+        self._owners = [o[4] for o in ctx.operands]
+        self._sc = (ctypes.c_double * max(1, len(ctx.scalars)))(*ctx.scalars)
+        self._keys = (ctypes.c_uint64 * max(1, len(ctx.keys)))(*ctx.keys)
+        a = _abi.AetherLaunch()
+        a.n = n
+        a.sample_offset = sample_offset
+        a.dst = dst_ptr or 0
+        a.dst_pitch = dst_pitch
+        a.operands = self._ops
+        a.n_operands = len(ctx.operands)
+        a.scalars = self._sc
+        a.n_scalars = len(ctx.scalars)
+        a.keys = self._keys
+        a.n_keys = len(ctx.keys)
+        a.reduce_out = reduce_ptr or 0
+        if workspace is not None:
+            a.workspace = workspace.data_ptr()
+            a.workspace_bytes = workspace.numel() * workspace.element_size()
+        self.args = a
+
+    def __call__(self, stream=None):
+        s = stream if stream is not None else _torch().cuda.current_stream().cuda_stream
+        _abi.check(_abi.lib().aether_plan_launch(self.plan.handle, ctypes.byref(self.args), ctypes.c_void_p(s)))
+
+
+def prepare(dst, expr, op="set", n=None, sample_offset=0, reduce_out=None, workspace=None, **low):
+    """Lower `dst <op>= expr` and bind its arguments; returns a Launch."""
+    if isinstance(expr, (int, float)):
+        expr = constant(expr, dst.shape)
+    ctx = IrContext()
+    if op in ("sum",):
+        dtype, shape = dst if isinstance(dst, tuple) else ("f64", ())
+        ir = plan_text(dtype, shape, op, expr, ctx)
+        n = int(n)
+        return Launch(get_plan(ir, **low), ctx, n, 0, 0, sample_offset, reduce_out.data_ptr(), workspace)
+    n = dst.n if n is None else int(n)
+    ir = plan_text(dst.dtype, dst.shape if dst.shape != (1,) or expr.shape == (1,) else (), op, expr, ctx)
+    red = reduce_out.data_ptr() if reduce_out is not None else None
+    return Launch(get_plan(ir, **low), ctx, n, dst.data.data_ptr(), dst.capacity, sample_offset, red, workspace)
+
+
+def assign(dst, expr, op="set", stream=None, **kw):
+    """dst[i] = expr for every sample i, in one kernel (expr/Assign.h:251-346)."""
+    L = prepare(dst, expr, op=op, **kw)
+    L(stream)
+    return dst
+
+
+def assign_add(dst, expr, **kw):
+    return assign(dst, expr, op="add", **kw)
+
+
+def assign_sub(dst, expr, **kw):
+    return assign(dst, expr, op="sub", **kw)
+
+
+def global_sum(expr, n, dtype="f64", stream=None, workspace=None, **kw):
+    """Compensated sum over samples of a rank-0 expression: returns a device
+    tensor (hi, comp), reduced in a fixed order (deterministic)."""
+    torch = _torch()
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    L = prepare((dtype, ()), expr, op="sum", n=n, reduce_out=out, workspace=workspace, **kw)
+    L(stream)
+    return out
+
+
+__all__ = [
+    "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
+    "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
+    "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",
+    "cwiseMax", "cwiseMin", "cwisePow", "cwiseRsqrt", "cwiseSign", "cwiseSin", "cwiseSqrt", "cwiseSquare", "cwiseTan",
+    "cwiseTanh", "splitmix64", "lowering",
+]

@@ -1,0 +1,128 @@
+"""In-tree build of libaether_gb300.so (the C-ABI engine).
+
+Host sources compile with g++, device sources with nvcc for sm_103a only; the
+device headers that generated kernels include are embedded as string
+literals. Translation units compile in parallel; nothing here needs cmake.
+
+usage: python -m aether_gb300.build [--force]
+"""
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIBDIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIBDIR, "libaether_gb300.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp"]
+DEVICE_SOURCES = []
+EMBED = [("kAgDeviceSrc", "device/ag_device.cuh"), ("kAgEmu64Src", "device/ag_emu64.cuh")]
+EXPORT_PREFIX = "aether_"
+
+
+def cuda_home():
+    for cand in (os.environ.get("CUDA_HOME"), os.environ.get("CUDA_PATH"), "/usr/local/cuda"):
+        if cand and os.path.exists(os.path.join(cand, "bin", "nvcc")):
+            return cand
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    raise RuntimeError("nvcc not found: set CUDA_HOME")
+
+
+def _write_if_changed(path, text):
+    if os.path.exists(path) and open(path).read() == text:
+        return
+    with open(path, "w") as f:
+        f.write(text)
+
+
+def _embed():
+    parts = ["// generated by aether_gb300/build.py from csrc/device/*.cuh\n"]
+    for name, rel in EMBED:
+        src = open(os.path.join(CSRC, rel)).read()
+        delim = "AGSRC"
+        assert ")" + delim + '"' not in src
+        # Raw literals are limited in length by some compilers: split in pieces.
+        pieces = [src[i:i + 12000] for i in range(0, len(src), 12000)] or [""]
+        body = "\n".join('R"%s(%s)%s"' % (delim, p, delim) for p in pieces)
+        parts.append("static const char* const %s =\n%s;\n" % (name, body))
+    _write_if_changed(os.path.join(BUILD, "embedded.inc"), "".join(parts))
+
+
+def _exports():
+    text = "{\n  global: %s*;\n  local: *;\n};\n" % EXPORT_PREFIX
+    _write_if_changed(os.path.join(BUILD, "exports.map"), text)
+
+
+def _stale(obj, deps):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    out = []
+    for root, _, files in os.walk(CSRC):
+        out += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh", ".inc"))]
+    out.append(os.path.join(REPO, "include", "aether_gb300.h"))
+    out.append(os.path.join(BUILD, "embedded.inc"))
+    return out
+
+
+def build(force=False, verbose=False):
+    cuda = cuda_home()
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    _embed()
+    _exports()
+    inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC, "-I" + BUILD, "-I" + os.path.join(cuda, "include")]
+    hdrs = _headers()
+    jobs = []
+    objs = []
+    for s in HOST_SOURCES:
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(BUILD, s + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + hdrs):
+            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wno-unused-function",
+                         "-c", src, "-o", obj] + inc)
+    for s in DEVICE_SOURCES:
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(BUILD, s + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + hdrs):
+            jobs.append([os.path.join(cuda, "bin", "nvcc"), ARCH, "-O3", "-std=c++17", "-lineinfo",
+                         "-Xcompiler", "-fPIC,-fvisibility=hidden", "-c", src, "-o", obj] + inc)
+    with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        futs = [ex.submit(subprocess.run, j, capture_output=True, text=True) for j in jobs]
+        for j, f in zip(jobs, futs):
+            r = f.result()
+            if verbose or r.returncode:
+                sys.stderr.write(" ".join(j) + "\n" + r.stdout + r.stderr)
+            if r.returncode:
+                raise RuntimeError("compile failed: " + j[-len(inc) - 1 if False else 0] + " " + " ".join(j[:6]))
+    if force or jobs or not os.path.exists(LIB):
+        libdir = os.path.join(cuda, "lib64")
+        if not os.path.isdir(libdir):
+            libdir = os.path.join(cuda, "lib")
+        cmd = ["g++", "-shared", "-o", LIB] + objs + [
+            "-L" + libdir, "-lcudart_static", "-lnvrtc", "-ldl", "-lpthread", "-lrt",
+            "-Wl,-rpath," + libdir, "-Wl,--version-script=" + os.path.join(BUILD, "exports.map"),
+            "-Wl,--no-undefined"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,506 @@
+// abi.cpp -- the extern "C" surface declared in include/aether_gb300.h.
+//
+// Memory entry points follow the reference seam (dsc/src/plugin.cpp:20-156):
+// status codes, a per-thread last error, device switching around each call.
+// Plan entry points own the parsed plan, its compiled module and, for sum
+// plans, a default workspace.
+
+#include "aether_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "jit.h"
+#include "plan.h"
+
+#define AG_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(const std::string& m) {
+    g_error = m;
+    return AETHER_FAIL;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    cudaGetLastError();
+    return fail(std::string(what) + ": " + cudaGetErrorString(e));
+}
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return AETHER_OK;
+    } catch (const std::exception& e) {
+        return fail(e.what());
+    }
+}
+
+struct OnDevice {
+    int prev = 0;
+    bool switched = false;
+    explicit OnDevice(int dev) {
+        cudaGetDevice(&prev);
+        switched = prev != dev;
+        if (switched) cudaSetDevice(dev);
+    }
+    ~OnDevice() {
+        if (switched) cudaSetDevice(prev);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Chunks (chunk/Chunk.h:111-260): host, pinned or stream-ordered device bytes.
+// ---------------------------------------------------------------------------
+struct Chunk {
+    int kind = AETHER_MEM_CPU;
+    int dev = 0;
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+};
+
+std::mutex g_deferred_mu;
+std::vector<Chunk*> g_deferred;
+
+void free_now(Chunk* c) {
+    if (c->ptr) {
+        if (c->kind == AETHER_MEM_CPU) std::free(c->ptr);
+        else if (c->kind == AETHER_MEM_PINNED) cudaFreeHost(c->ptr);
+        else {
+            OnDevice d(c->dev);
+            cudaFreeAsync(c->ptr, c->stream);
+        }
+    }
+    delete c;
+}
+
+bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return st != cudaStreamCaptureStatusNone;
+}
+
+// ---------------------------------------------------------------------------
+// Plans.
+// ---------------------------------------------------------------------------
+
+// Host image of the device's AgArgs (csrc/device/ag_device.cuh); the kernel
+// receives it by value.
+struct AgArgsHost {
+    uint64_t n;
+    uint32_t offset, flags;
+    char* dst;
+    uint64_t dst_pitch;
+    const char* ops[16];
+    uint64_t pitch[16];
+    double sc[16];
+    uint64_t key[8];
+    double* red;
+    char* ws;
+    uint64_t ws_bytes;
+};
+static_assert(sizeof(AgArgsHost) == 504, "AgArgs layout");
+
+struct PlanObj {
+    ag::Plan plan;
+    ag::Lowering low;
+    std::string source;
+    ag::Compiled compiled;
+    cudaLibrary_t library = nullptr;
+    cudaKernel_t fv = nullptr, fs = nullptr;
+    int vec = 2;
+    int registers = 0;
+    int blocks_per_sm_v = 1, blocks_per_sm_s = 1;
+    int sms = 1;
+    int dev = 0;
+    // default workspace of sum plans
+    std::mutex ws_mu;
+    void* ws = nullptr;
+    size_t ws_bytes = 0;
+};
+
+ag::Lowering default_lowering(const ag::Plan& p) {
+    ag::Lowering l;
+    l.block = 256;
+    l.ipt = 1;
+    l.vec = 0;
+    l.contract = true;
+    l.math = 0;
+    (void)p;
+    return l;
+}
+
+uint64_t chunk_samples(const PlanObj& P, bool vectorized) {
+    return uint64_t(P.low.block) * uint64_t(P.low.ipt) * uint64_t(vectorized ? P.vec : 1);
+}
+
+uint64_t ws_needed(const PlanObj& P, uint64_t n) {
+    if (!P.plan.wants_sum()) return 0;
+    const uint64_t per = chunk_samples(P, false);   // the scalar kernel has the most chunks
+    const uint64_t nch = (n + per - 1) / per;
+    return 16 + 16 * std::max<uint64_t>(nch, 1);
+}
+
+}  // namespace
+
+// ============================================================================
+// Memory
+// ============================================================================
+AG_EXPORT int aether_probe(int* count) {
+    int n = 0;
+    const cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (n < 1) return fail("no CUDA device");
+    if (count) *count = n;
+    return AETHER_OK;
+}
+
+AG_EXPORT int aether_runtime_version(int* v) {
+    const cudaError_t e = cudaRuntimeGetVersion(v);
+    return e == cudaSuccess ? AETHER_OK : cuda_fail(e, "cudaRuntimeGetVersion");
+}
+
+AG_EXPORT const char* aether_last_error(void) { return g_error.c_str(); }
+
+AG_EXPORT int aether_chunk_alloc(int kind, int dev, size_t bytes, void* stream, void** chunk, void** ptr) {
+    return guarded([&] {
+        if (!chunk || !ptr) throw std::runtime_error("chunk_alloc: null output pointer");
+        auto c = std::make_unique<Chunk>();
+        c->kind = kind;
+        c->dev = dev;
+        c->bytes = bytes;
+        c->stream = static_cast<cudaStream_t>(stream);
+        const size_t b = std::max<size_t>(bytes, 1);
+        if (kind == AETHER_MEM_CPU) {
+            c->ptr = std::aligned_alloc(256, (b + 255) / 256 * 256);
+            if (!c->ptr) throw std::runtime_error("chunk_alloc failed on cpu, size=" + std::to_string(bytes) + " bytes");
+        } else if (kind == AETHER_MEM_PINNED) {
+            ck(cudaMallocHost(&c->ptr, b), "cudaMallocHost");
+        } else if (kind == AETHER_MEM_DEVICE) {
+            OnDevice d(dev);
+            ck(cudaMallocAsync(&c->ptr, b, c->stream), "cudaMallocAsync");
+        } else {
+            throw std::runtime_error("chunk_alloc: unknown memory kind " + std::to_string(kind));
+        }
+        *ptr = c->ptr;
+        *chunk = c.release();
+    });
+}
+
+AG_EXPORT void aether_chunk_release(void* chunk) {
+    Chunk* c = static_cast<Chunk*>(chunk);
+    if (!c) return;
+    if (c->kind == AETHER_MEM_DEVICE && capturing(c->stream)) {
+        std::lock_guard<std::mutex> lk(g_deferred_mu);
+        g_deferred.push_back(c);
+        return;
+    }
+    free_now(c);
+}
+
+AG_EXPORT void aether_drain(void) {
+    std::vector<Chunk*> keep, now;
+    {
+        std::lock_guard<std::mutex> lk(g_deferred_mu);
+        for (Chunk* c : g_deferred) (capturing(c->stream) ? keep : now).push_back(c);
+        g_deferred.swap(keep);
+    }
+    for (Chunk* c : now) free_now(c);
+}
+
+AG_EXPORT int aether_fill(int kind, int dev, void* ptr, size_t bytes, const void* value, size_t width, void* stream) {
+    return guarded([&] {
+        if (!ptr || (!value && width) || width == 0 || bytes % width)
+            throw std::runtime_error("fill: bytes must be a multiple of a non-zero width");
+        const unsigned char* v = static_cast<const unsigned char*>(value);
+        bool uniform = true;
+        for (size_t i = 1; i < width; ++i) uniform = uniform && v[i] == v[0];
+        if (kind == AETHER_MEM_CPU || kind == AETHER_MEM_PINNED) {
+            if (kind == AETHER_MEM_PINNED && stream) ck(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "sync");
+            unsigned char* p = static_cast<unsigned char*>(ptr);
+            for (size_t off = 0; off < bytes; off += width) std::memcpy(p + off, v, width);
+            return;
+        }
+        OnDevice d(dev);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (uniform) {
+            ck(cudaMemsetAsync(ptr, v[0], bytes, s), "cudaMemsetAsync");
+        } else {
+            // Non-uniform patterns: seed one copy, then double it with device copies.
+            ck(cudaMemcpyAsync(ptr, value, width, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+            size_t done = width;
+            unsigned char* p = static_cast<unsigned char*>(ptr);
+            while (done < bytes) {
+                const size_t n = std::min(done, bytes - done);
+                ck(cudaMemcpyAsync(p + done, p, n, cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+                done += n;
+            }
+        }
+    });
+}
+
+AG_EXPORT int aether_copy(int dst_kind, int dst_dev, void* dst, int src_kind, int src_dev, const void* src,
+                          size_t bytes, void* stream) {
+    return guarded([&] {
+        if (bytes == 0) return;
+        if (!dst || !src) throw std::runtime_error("copy: null pointer");
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const bool dd = dst_kind == AETHER_MEM_DEVICE, sd = src_kind == AETHER_MEM_DEVICE;
+        if (!dd && !sd && dst_kind != AETHER_MEM_PINNED && src_kind != AETHER_MEM_PINNED) {
+            std::memcpy(dst, src, bytes);
+            return;
+        }
+        if (dd && sd && dst_dev != src_dev) {
+            ck(cudaMemcpyPeerAsync(dst, dst_dev, src, src_dev, bytes, s), "cudaMemcpyPeerAsync");
+            return;
+        }
+        OnDevice d(dd ? dst_dev : src_dev);
+        const cudaMemcpyKind k = dd && sd ? cudaMemcpyDeviceToDevice
+                                 : dd     ? cudaMemcpyHostToDevice
+                                 : sd     ? cudaMemcpyDeviceToHost
+                                          : cudaMemcpyHostToHost;
+        ck(cudaMemcpyAsync(dst, src, bytes, k, s), "cudaMemcpyAsync");
+    });
+}
+
+AG_EXPORT int aether_stream_wait(int dev, void* producer, void* consumer) {
+    return guarded([&] {
+        OnDevice d(dev);
+        cudaEvent_t ev;
+        ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+        cudaError_t e = cudaEventRecord(ev, static_cast<cudaStream_t>(producer));
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(static_cast<cudaStream_t>(consumer), ev, 0);
+        cudaEventDestroy(ev);
+        ck(e, "stream_wait");
+    });
+}
+
+AG_EXPORT int aether_stream_sync(int dev, void* stream) {
+    return guarded([&] {
+        OnDevice d(dev);
+        ck(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "cudaStreamSynchronize");
+    });
+}
+
+// ============================================================================
+// Plans
+// ============================================================================
+AG_EXPORT int aether_plan_create(const char* ir, const AetherLowering* lowering, void** out) {
+    return guarded([&] {
+        if (!ir || !out) throw std::runtime_error("plan_create: null argument");
+        auto P = std::make_unique<PlanObj>();
+        P->plan = ag::parse_plan(ir);
+        P->low = default_lowering(P->plan);
+        if (lowering) {
+            if (lowering->block > 0) P->low.block = lowering->block;
+            if (lowering->ipt > 0) P->low.ipt = lowering->ipt;
+            if (lowering->vec > 0) P->low.vec = lowering->vec;
+            if (lowering->contract >= 0) P->low.contract = lowering->contract != 0;
+            if (lowering->math >= 0) P->low.math = lowering->math;
+            if (lowering->min_blocks > 0) P->low.min_blocks = lowering->min_blocks;
+        }
+        if (P->low.block % 32 || P->low.block < 32 || P->low.block > 1024)
+            throw std::runtime_error("plan_create: block must be a multiple of 32 in [32, 1024]");
+        if (P->low.ipt < 1 || P->low.ipt > 8) throw std::runtime_error("plan_create: ipt must be in [1, 8]");
+        P->vec = ag::effective_vec(P->plan, P->low);
+        if (P->vec != 1 && P->vec != 2 && P->vec != 4) throw std::runtime_error("plan_create: vec must be 1, 2 or 4");
+        if (P->low.math == 1 && P->plan.dst_dtype != ag::DType::F64)
+            throw std::runtime_error("plan_create: emulated FP64 applies to f64 plans");
+        P->source = ag::generate_source(P->plan, P->low);
+        ck(cudaFree(nullptr), "CUDA context");   // make the primary context current
+        cudaGetDevice(&P->dev);
+        P->compiled = ag::compile_cached(P->source, "plan");
+        ck(cudaLibraryLoadData(&P->library, P->compiled.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+           "cudaLibraryLoadData");
+        ck(cudaLibraryGetKernel(&P->fv, P->library, "ag_plan_v"), "cudaLibraryGetKernel(ag_plan_v)");
+        ck(cudaLibraryGetKernel(&P->fs, P->library, "ag_plan_s"), "cudaLibraryGetKernel(ag_plan_s)");
+        cudaFuncAttributes fa{};
+        ck(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(P->fv)), "cudaFuncGetAttributes");
+        P->registers = fa.numRegs;
+        ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&P->blocks_per_sm_v, reinterpret_cast<const void*>(P->fv),
+                                                         P->low.block, 0), "occupancy");
+        ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&P->blocks_per_sm_s, reinterpret_cast<const void*>(P->fs),
+                                                         P->low.block, 0), "occupancy");
+        cudaDeviceGetAttribute(&P->sms, cudaDevAttrMultiProcessorCount, P->dev);
+        *out = P.release();
+    });
+}
+
+AG_EXPORT int aether_plan_info(void* plan, AetherPlanInfo* info) {
+    return guarded([&] {
+        const PlanObj* P = static_cast<const PlanObj*>(plan);
+        if (!P || !info) throw std::runtime_error("plan_info: null argument");
+        info->hash = P->compiled.hash;
+        info->n_operands = P->plan.n_operands;
+        info->n_scalars = P->plan.n_scalars;
+        info->n_keys = P->plan.n_keys;
+        info->dst_comps = P->plan.dst_comps;
+        info->dst_dtype = P->plan.dst_dtype == ag::DType::F64 ? 0 : P->plan.dst_dtype == ag::DType::F32 ? 1 : 2;
+        info->is_sum = P->plan.wants_sum() ? 1 : 0;
+        info->block = P->low.block;
+        info->ipt = P->low.ipt;
+        info->vec = P->vec;
+        info->registers = P->registers;
+        info->blocks_per_sm = P->blocks_per_sm_v;
+        info->compile_ms = P->compiled.compile_ms;
+    });
+}
+
+AG_EXPORT int aether_plan_workspace_size(void* plan, uint64_t n, uint64_t* bytes) {
+    return guarded([&] {
+        const PlanObj* P = static_cast<const PlanObj*>(plan);
+        if (!P || !bytes) throw std::runtime_error("plan_workspace_size: null argument");
+        *bytes = ws_needed(*P, n);
+    });
+}
+
+AG_EXPORT int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len) {
+    return guarded([&] {
+        const PlanObj* P = static_cast<const PlanObj*>(plan);
+        if (!P) throw std::runtime_error("plan_source: null plan");
+        if (len) *len = P->source.size();
+        if (buf && cap) {
+            const size_t n = std::min(cap - 1, P->source.size());
+            std::memcpy(buf, P->source.data(), n);
+            buf[n] = '\0';
+        }
+    });
+}
+
+AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream) {
+    return guarded([&] {
+        PlanObj* P = static_cast<PlanObj*>(plan);
+        if (!P || !a) throw std::runtime_error("plan_launch: null argument");
+        const ag::Plan& pl = P->plan;
+        if (a->n == 0) return;
+        if (a->n > 0xFFFFFFFFull) throw std::runtime_error("plan_launch: n exceeds the 32-bit sample index");
+        if (uint64_t(a->sample_offset) + a->n - 1 > 0xFFFFFFFFull)
+            throw std::runtime_error("plan_launch: sample_offset + n exceeds the 32-bit sample index");
+        if (int(a->n_operands) < pl.n_operands)
+            throw std::runtime_error("plan_launch: plan reads " + std::to_string(pl.n_operands) + " operands, " +
+                                     std::to_string(a->n_operands) + " given");
+        if (int(a->n_scalars) < pl.n_scalars) throw std::runtime_error("plan_launch: too few scalars");
+        if (int(a->n_keys) < pl.n_keys) throw std::runtime_error("plan_launch: too few generator keys");
+        AgArgsHost k{};
+        k.n = a->n;
+        k.offset = a->sample_offset;
+        bool aligned = true;
+        if (pl.wants_store()) {
+            if (!a->dst) throw std::runtime_error("plan_launch: null destination");
+            if (pl.dst_comps > 1 && a->dst_pitch < a->n)
+                throw std::runtime_error("plan_launch: destination pitch smaller than n");
+            k.dst = static_cast<char*>(a->dst);
+            k.dst_pitch = a->dst_pitch ? a->dst_pitch : a->n;
+            const int es = ag::dtype_size(pl.dst_dtype);
+            aligned = aligned && (reinterpret_cast<uintptr_t>(a->dst) % 16 == 0) &&
+                      (pl.dst_comps == 1 || (k.dst_pitch * es) % 16 == 0);
+        }
+        for (int i = 0; i < pl.n_operands; ++i) {
+            const AetherOperand& o = a->operands[i];
+            if (!o.ptr) throw std::runtime_error("plan_launch: operand " + std::to_string(i) + " is null");
+            const int comps = pl.operand_comps[size_t(i)];
+            const uint64_t pitch = o.pitch ? o.pitch : a->n;
+            if (comps > 1 && pitch < a->n)
+                throw std::runtime_error("plan_launch: operand " + std::to_string(i) + " pitch smaller than n");
+            k.ops[i] = static_cast<const char*>(o.ptr);
+            k.pitch[i] = pitch;
+            const int es = ag::dtype_size(pl.operand_dtype[size_t(i)]);
+            aligned = aligned && (reinterpret_cast<uintptr_t>(o.ptr) % 16 == 0) && (comps == 1 || (pitch * es) % 16 == 0);
+        }
+        for (int i = 0; i < pl.n_scalars; ++i) k.sc[i] = a->scalars[i];
+        for (int i = 0; i < pl.n_keys; ++i) k.key[i] = a->keys[i];
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const bool vect = aligned && P->vec > 1;
+        if (pl.wants_sum()) {
+            if (!a->reduce_out) throw std::runtime_error("plan_launch: sum plan without reduce_out");
+            k.red = a->reduce_out;
+            const uint64_t need = ws_needed(*P, a->n);
+            if (a->workspace) {
+                if (a->workspace_bytes < need)
+                    throw std::runtime_error("plan_launch: workspace of " + std::to_string(a->workspace_bytes) +
+                                             " bytes, " + std::to_string(need) + " needed");
+                k.ws = static_cast<char*>(a->workspace);
+                k.ws_bytes = a->workspace_bytes;
+            } else {
+                std::lock_guard<std::mutex> lk(P->ws_mu);
+                if (P->ws_bytes < need) {
+                    if (P->ws) ck(cudaFree(P->ws), "cudaFree");
+                    P->ws = nullptr;
+                    P->ws_bytes = 0;
+                    ck(cudaMalloc(&P->ws, need), "cudaMalloc(workspace)");
+                    P->ws_bytes = need;
+                }
+                k.ws = static_cast<char*>(P->ws);
+                k.ws_bytes = P->ws_bytes;
+            }
+            ck(cudaMemsetAsync(k.ws, 0, 16, s), "cudaMemsetAsync(counter)");
+        }
+        const uint64_t per = chunk_samples(*P, vect);
+        const uint64_t nch = (a->n + per - 1) / per;
+        const int bps = vect ? P->blocks_per_sm_v : P->blocks_per_sm_s;
+        const uint64_t cap = uint64_t(std::max(bps, 1)) * uint64_t(P->sms);
+        const unsigned grid = unsigned(std::max<uint64_t>(1, std::min(nch, cap)));
+        void* params[] = {&k};
+        ck(cudaLaunchKernel(reinterpret_cast<const void*>(vect ? P->fv : P->fs), dim3(grid), dim3(unsigned(P->low.block)),
+                            params, 0, s),
+           "cudaLaunchKernel");
+    });
+}
+
+AG_EXPORT int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* buf, size_t cap,
+                                   size_t* len) {
+    return guarded([&] {
+        if (!ir) throw std::runtime_error("plan_generate: null ir");
+        const ag::Plan plan = ag::parse_plan(ir);
+        ag::Lowering low = default_lowering(plan);
+        if (lowering) {
+            if (lowering->block > 0) low.block = lowering->block;
+            if (lowering->ipt > 0) low.ipt = lowering->ipt;
+            if (lowering->vec > 0) low.vec = lowering->vec;
+            if (lowering->contract >= 0) low.contract = lowering->contract != 0;
+            if (lowering->math >= 0) low.math = lowering->math;
+            if (lowering->min_blocks > 0) low.min_blocks = lowering->min_blocks;
+        }
+        const std::string src = ag::generate_source(plan, low);
+        if (len) *len = src.size();
+        if (buf && cap) {
+            const size_t n = std::min(cap - 1, src.size());
+            std::memcpy(buf, src.data(), n);
+            buf[n] = '\0';
+        }
+    });
+}
+
+AG_EXPORT int aether_nvrtc_check(const char* source, const char* arch) {
+    return guarded([&] {
+        if (!source || !arch) throw std::runtime_error("nvrtc_check: null argument");
+        ag::compile_for_arch(source, arch);
+    });
+}
+
+AG_EXPORT void aether_plan_release(void* plan) {
+    PlanObj* P = static_cast<PlanObj*>(plan);
+    if (!P) return;
+    if (P->ws) cudaFree(P->ws);
+    if (P->library) cudaLibraryUnload(P->library);
+    delete P;
+}

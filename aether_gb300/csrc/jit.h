@@ -1,0 +1,29 @@
+// jit.h -- NVRTC compilation of generated plan kernels, cached by hash in
+// memory and on disk, loaded through the driver API.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+namespace ag {
+
+struct Compiled {
+    std::string cubin;
+    double compile_ms = 0.0;   // 0 when served from a cache
+    uint64_t hash = 0;
+};
+
+uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ULL);
+
+// Compile `source` (which may include "ag_device.cuh" / "ag_emu64.cuh") for
+// the current device's architecture. Throws std::runtime_error with the NVRTC
+// log on failure.
+Compiled compile_cached(const std::string& source, const std::string& tag);
+
+// The architecture string of the current device, e.g. "sm_103a".
+std::string current_arch();
+
+// Compile for `arch` without caching or loading (offline checks).
+std::string compile_for_arch(const std::string& source, const std::string& arch);
+
+}  // namespace ag

@@ -1,0 +1,817 @@
+// plan.cpp -- aether-ir/1 parser, shape checker and CUDA generator.
+//
+// The grammar is an S-expression over the node kinds of the reference's
+// expression layer (expr/nodes/*.h, expr/Reduce.h, random/detail/
+// DistributionLeaf.h). Each generated formula keeps the reference's operand
+// order and association, so with contraction off the arithmetic nodes round
+// exactly as the reference's `-ffp-contract=off` CPU build does.
+
+#include "plan.h"
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <sstream>
+#include <stdexcept>
+
+namespace ag {
+
+const char* dtype_name(DType d) {
+    switch (d) {
+    case DType::F64: return "f64";
+    case DType::F32: return "f32";
+    case DType::FF: return "ff";
+    case DType::I32: return "i32";
+    case DType::U8: return "u8";
+    }
+    return "?";
+}
+int dtype_size(DType d) {
+    switch (d) {
+    case DType::F64: return 8;
+    case DType::F32: return 4;
+    case DType::FF: return 4;
+    case DType::I32: return 4;
+    case DType::U8: return 1;
+    }
+    return 8;
+}
+
+namespace {
+
+[[noreturn]] void fail(const std::string& m) { throw std::runtime_error("aether-ir: " + m); }
+
+DType parse_dtype(const std::string& t) {
+    if (t == "f64") return DType::F64;
+    if (t == "f32") return DType::F32;
+    if (t == "ff") return DType::FF;
+    if (t == "i32") return DType::I32;
+    if (t == "u8") return DType::U8;
+    fail("unknown dtype '" + t + "'");
+}
+
+std::vector<int> parse_shape(const std::string& t) {
+    if (t.size() < 2 || t.front() != '[' || t.back() != ']') fail("bad shape '" + t + "'");
+    std::vector<int> s;
+    const std::string inner = t.substr(1, t.size() - 2);
+    size_t i = 0;
+    while (i < inner.size()) {
+        size_t j = inner.find(',', i);
+        if (j == std::string::npos) j = inner.size();
+        const int v = std::stoi(inner.substr(i, j - i));
+        if (v <= 0 || v > 64) fail("extent out of range in " + t);
+        s.push_back(v);
+        i = j + 1;
+    }
+    if (s.size() > 2) fail("rank > 2 element shapes are not supported: " + t);
+    return s;
+}
+
+int prod(const std::vector<int>& s) {
+    int p = 1;
+    for (int v : s) p *= v;
+    return p;
+}
+
+const std::set<std::string>& unary_ops() {
+    static const std::set<std::string> s = {"neg", "abs", "sign", "sqrt", "rsqrt", "exp", "expm1", "log", "log1p",
+                                            "log2", "log10", "exp2", "sin", "cos", "tan", "asin", "acos", "atan",
+                                            "tanh", "sinh", "cosh", "sq", "floor", "ceil", "trunc", "cbrt", "erf"};
+    return s;
+}
+const std::set<std::string>& binary_ops() {
+    static const std::set<std::string> s = {"add", "sub", "mul", "div", "pow", "min", "max", "atan2", "hypot"};
+    return s;
+}
+const std::set<std::string>& cmp_ops() {
+    static const std::set<std::string> s = {"gt", "lt", "ge", "le", "eq", "ne", "and", "or"};
+    return s;
+}
+
+struct Parser {
+    const char* p;
+    const char* begin;
+    Plan plan;
+    std::map<std::string, int> memo;
+    int ctx = 0;   // 0: the lane's own sample; 1: sample 0 (inside at0)
+    std::vector<int> node_ctx;
+
+    explicit Parser(const char* s) : p(s), begin(s) {}
+
+    void ws() {
+        while (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r') ++p;
+    }
+    std::string tok() {
+        ws();
+        if (!*p) fail("unexpected end of text");
+        if (*p == '(' || *p == ')') return std::string(1, *p++);
+        const char* s = p;
+        if (*p == '[') {
+            while (*p && *p != ']') ++p;
+            if (*p != ']') fail("unterminated shape");
+            ++p;
+            return std::string(s, p);
+        }
+        while (*p && *p != ' ' && *p != '(' && *p != ')' && *p != '\n' && *p != '\t' && *p != '\r') ++p;
+        return std::string(s, p);
+    }
+    std::string peek() {
+        const char* save = p;
+        std::string t = tok();
+        p = save;
+        return t;
+    }
+    void expect(const char* t) {
+        const std::string g = tok();
+        if (g != t) fail(std::string("expected '") + t + "' but found '" + g + "' at offset " + std::to_string(p - begin));
+    }
+    int integer() {
+        const std::string t = tok();
+        char* end = nullptr;
+        const long v = std::strtol(t.c_str(), &end, 10);
+        if (!end || *end) fail("expected an integer, found '" + t + "'");
+        return int(v);
+    }
+    const Node& N(int i) const { return plan.nodes[size_t(i)]; }
+
+    int expr() {
+        const char* start = p;
+        expect("(");
+        Node n;
+        n.op = tok();
+        const std::string op = n.op;
+        auto kid = [&]() {
+            const int c = expr();
+            n.kids.push_back(c);
+            return c;
+        };
+        auto same_shape = [&](int a, int b) {
+            if (N(a).shape != N(b).shape) fail("operand shapes differ in '" + op + "'");
+        };
+        auto rank0 = [&](int a) {
+            if (!N(a).shape.empty()) fail("'" + op + "' needs a rank-0 operand");
+        };
+        auto num = [&](int a) {
+            if (N(a).is_bool) fail("'" + op + "' needs a numeric operand");
+        };
+        if (op == "in") {
+            n.k = integer();
+            if (n.k < 0 || n.k >= 16) fail("operand slot out of range");
+            n.dtype = parse_dtype(tok());
+            n.shape = parse_shape(tok());
+            if (plan.n_operands <= n.k) {
+                plan.n_operands = n.k + 1;
+                plan.operand_dtype.resize(size_t(n.k) + 1, DType::F64);
+                plan.operand_comps.resize(size_t(n.k) + 1, 0);
+            }
+            if (plan.operand_comps[size_t(n.k)] && (plan.operand_comps[size_t(n.k)] != prod(n.shape) ||
+                                                    plan.operand_dtype[size_t(n.k)] != n.dtype))
+                fail("operand " + std::to_string(n.k) + " declared twice with different types");
+            plan.operand_comps[size_t(n.k)] = prod(n.shape);
+            plan.operand_dtype[size_t(n.k)] = n.dtype;
+            n.is_bool = n.dtype == DType::U8;
+        } else if (op == "sc") {
+            n.k = integer();
+            if (n.k < 0 || n.k >= 16) fail("scalar slot out of range");
+            plan.n_scalars = std::max(plan.n_scalars, n.k + 1);
+        } else if (op == "lit") {
+            const std::string t = tok();
+            char* end = nullptr;
+            n.lit = std::strtod(t.c_str(), &end);
+            if (!end || *end) fail("bad literal '" + t + "'");
+        } else if (op == "bcast") {
+            const int a = kid();
+            rank0(a);
+            n.shape = parse_shape(tok());
+            n.is_bool = N(a).is_bool;
+        } else if (op == "at0") {
+            const int save = ctx;
+            ctx = 1;
+            const int a = kid();
+            ctx = save;
+            n.shape = N(a).shape;
+            n.is_bool = N(a).is_bool;
+        } else if (unary_ops().count(op)) {
+            const int a = kid();
+            num(a);
+            n.shape = N(a).shape;
+        } else if (binary_ops().count(op)) {
+            const int a = kid(), b = kid();
+            same_shape(a, b);
+            num(a);
+            num(b);
+            n.shape = N(a).shape;
+        } else if (op == "scale" || op == "mins" || op == "maxs" || op == "pows") {
+            const int a = kid(), s = kid();
+            rank0(s);
+            n.shape = N(a).shape;
+        } else if (op == "clamp") {
+            const int a = kid(), lo = kid(), hi = kid();
+            rank0(lo);
+            rank0(hi);
+            n.shape = N(a).shape;
+        } else if (cmp_ops().count(op)) {
+            const int a = kid(), b = kid();
+            same_shape(a, b);
+            n.shape = N(a).shape;
+            n.is_bool = true;
+        } else if (op == "not") {
+            const int a = kid();
+            n.shape = N(a).shape;
+            n.is_bool = true;
+        } else if (op == "select") {
+            const int c = kid(), a = kid(), b = kid();
+            same_shape(a, b);
+            if (!N(c).is_bool) fail("select condition must be boolean");
+            if (!N(c).shape.empty() && N(c).shape != N(a).shape) fail("select condition shape");
+            n.shape = N(a).shape;
+            n.is_bool = N(a).is_bool;
+        } else if (op == "comp") {
+            const int a = kid();
+            n.k = integer();
+            if (n.k < 0 || n.k >= N(a).comps) fail("comp index out of range");
+        } else if (op == "seg") {
+            const int a = kid();
+            n.k = integer();
+            n.ints = {integer()};
+            if (N(a).shape.size() != 1 || n.k < 0 || n.ints[0] <= 0 || n.k + n.ints[0] > N(a).comps)
+                fail("seg out of range");
+            n.shape = {n.ints[0]};
+        } else if (op == "row" || op == "col") {
+            const int a = kid();
+            n.k = integer();
+            if (N(a).shape.size() != 2) fail(op + " needs a matrix");
+            const int lim = op == "row" ? N(a).shape[0] : N(a).shape[1];
+            if (n.k < 0 || n.k >= lim) fail(op + " index out of range");
+            n.shape = {op == "row" ? N(a).shape[1] : N(a).shape[0]};
+        } else if (op == "transpose") {
+            const int a = kid();
+            if (N(a).shape.size() != 2) fail("transpose needs a matrix");
+            n.shape = {N(a).shape[1], N(a).shape[0]};
+        } else if (op == "block") {
+            const int a = kid();
+            n.ints = {integer(), integer(), integer(), integer()};
+            if (N(a).shape.size() != 2 || n.ints[0] + n.ints[2] > N(a).shape[0] || n.ints[1] + n.ints[3] > N(a).shape[1])
+                fail("block out of range");
+            n.shape = {n.ints[2], n.ints[3]};
+        } else if (op == "stack") {
+            while (peek() != ")") rank0(kid());
+            if (n.kids.empty()) fail("empty stack");
+            n.shape = {int(n.kids.size())};
+        } else if (op == "reshape") {
+            const int a = kid();
+            n.shape = parse_shape(tok());
+            if (prod(n.shape) != N(a).comps) fail("reshape changes the component count");
+        } else if (op == "cross") {
+            const int a = kid(), b = kid();
+            same_shape(a, b);
+            if (N(a).shape != std::vector<int>{3}) fail("cross needs [3] operands");
+            n.shape = {3};
+        } else if (op == "unit") {
+            const int a = kid();
+            if (N(a).shape.size() != 1) fail("unit needs a vector");
+            n.shape = N(a).shape;
+        } else if (op == "qconj") {
+            const int a = kid();
+            if (N(a).shape != std::vector<int>{4}) fail("qconj needs [4]");
+            n.shape = {4};
+        } else if (op == "qmul") {
+            const int a = kid(), b = kid();
+            if (N(a).shape != std::vector<int>{4} || N(b).shape != std::vector<int>{4}) fail("qmul needs [4] operands");
+            n.shape = {4};
+        } else if (op == "qrot") {
+            const int a = kid(), b = kid();
+            if (N(a).shape != std::vector<int>{4} || N(b).shape != std::vector<int>{3}) fail("qrot needs [4] and [3]");
+            n.shape = {3};
+        } else if (op == "pureq") {
+            const int a = kid();
+            if (N(a).shape != std::vector<int>{3}) fail("pureq needs [3]");
+            n.shape = {4};
+        } else if (op == "inv" || op == "det" || op == "trace") {
+            const int a = kid();
+            const auto& s = N(a).shape;
+            if (s.size() != 2 || s[0] != s[1] || (s[0] != 2 && s[0] != 3)) fail(op + " needs a 2x2 or 3x3 matrix");
+            if (op == "inv") n.shape = s;
+        } else if (op == "matvec") {
+            const int m = kid(), v = kid();
+            if (N(m).shape.size() != 2 || N(v).shape.size() != 1 || N(m).shape[1] != N(v).shape[0]) fail("matvec shapes");
+            n.shape = {N(m).shape[0]};
+        } else if (op == "matmul") {
+            const int a = kid(), b = kid();
+            if (N(a).shape.size() != 2 || N(b).shape.size() != 2 || N(a).shape[1] != N(b).shape[0]) fail("matmul shapes");
+            n.shape = {N(a).shape[0], N(b).shape[1]};
+        } else if (op == "outer") {
+            const int a = kid(), b = kid();
+            if (N(a).shape.size() != 1 || N(b).shape.size() != 1) fail("outer needs vectors");
+            n.shape = {N(a).shape[0], N(b).shape[0]};
+        } else if (op == "dot") {
+            const int a = kid(), b = kid();
+            same_shape(a, b);
+            if (N(a).shape.size() != 1) fail("dot needs vectors");
+        } else if (op == "sqnorm" || op == "norm" || op == "rnorm" || op == "sum" || op == "maxnorm") {
+            const int a = kid();
+            if (N(a).shape.size() != 1) fail(op + " needs a vector");
+        } else if (op == "uniform" || op == "normal" || op == "lognormal" || op == "exponential" || op == "bernoulli") {
+            n.k = integer();
+            if (n.k < 0 || n.k >= 8) fail("key slot out of range");
+            plan.n_keys = std::max(plan.n_keys, n.k + 1);
+            const int p0 = kid();
+            const bool two = op == "uniform" || op == "normal" || op == "lognormal";
+            const int p1 = two ? kid() : -1;
+            const int vd = integer();
+            if (vd <= 0 || vd > 64) fail("distribution dimension out of range");
+            n.shape = {vd};
+            for (int q : {p0, p1}) {
+                if (q < 0) continue;
+                if (!N(q).shape.empty() && N(q).shape != n.shape) fail(op + " parameter shape");
+            }
+            plan.has_random = true;
+        } else {
+            fail("unknown node '" + op + "'");
+        }
+        expect(")");
+        n.comps = prod(n.shape);
+        const std::string key = std::to_string(ctx) + std::string(start, p);
+        auto it = memo.find(key);
+        if (it != memo.end()) return it->second;
+        plan.nodes.push_back(std::move(n));
+        node_ctx.push_back(ctx);
+        const int id = int(plan.nodes.size()) - 1;
+        memo.emplace(key, id);
+        return id;
+    }
+
+    Plan run() {
+        expect("(");
+        expect("plan");
+        plan.dst_dtype = parse_dtype(tok());
+        if (plan.dst_dtype != DType::F64 && plan.dst_dtype != DType::F32 && plan.dst_dtype != DType::FF)
+            fail("destination dtype must be f64, f32 or ff");
+        plan.dst_shape = parse_shape(tok());
+        plan.dst_comps = prod(plan.dst_shape);
+        plan.op = tok();
+        if (plan.op != "set" && plan.op != "add" && plan.op != "sub" && plan.op != "sum" && plan.op != "setsum")
+            fail("unknown assignment '" + plan.op + "'");
+        plan.root = expr();
+        expect(")");
+        ws();
+        if (*p) fail("trailing text after the plan");
+        if (N(plan.root).shape != plan.dst_shape) fail("expression shape does not match the destination");
+        if (N(plan.root).is_bool) fail("a boolean expression cannot be stored");
+        if (plan.wants_sum() && plan.dst_comps != 1) fail("sum plans need a rank-0 (or [1]) expression");
+        for (int k = 0; k < plan.n_operands; ++k)
+            if (!plan.operand_comps[size_t(k)]) fail("operand slot " + std::to_string(k) + " is unused");
+        return plan;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Code generation.
+// ---------------------------------------------------------------------------
+std::string hexlit(double v) {
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%a", v);
+    return buf;
+}
+
+struct Gen {
+    const Plan& P;
+    const Lowering& L;
+    std::vector<int> ctx;
+    std::string W;        // working type
+    std::string S;        // destination storage type
+    std::vector<std::vector<std::string>> val;
+    std::vector<char> done;
+    std::ostringstream pro;   // sample-0 prologue (at0 subtrees)
+    std::ostringstream body;  // per-lane code
+    int lane_ctx = 0;
+
+    Gen(const Plan& p, const Lowering& l, const std::vector<int>& c) : P(p), L(l), ctx(c), val(p.nodes.size()),
+                                                                         done(p.nodes.size(), 0) {
+        W = P.dst_dtype == DType::F64 ? "double" : "float";
+        S = P.dst_dtype == DType::F64 ? "double" : "float";
+    }
+
+    std::string add(const std::string& a, const std::string& b) const {
+        return L.contract ? "(" + a + " + " + b + ")" : "ag::rn_add(" + a + ", " + b + ")";
+    }
+    std::string sub(const std::string& a, const std::string& b) const {
+        return L.contract ? "(" + a + " - " + b + ")" : "ag::rn_sub(" + a + ", " + b + ")";
+    }
+    std::string mul(const std::string& a, const std::string& b) const {
+        return L.contract ? "(" + a + " * " + b + ")" : "ag::rn_mul(" + a + ", " + b + ")";
+    }
+    std::string div(const std::string& a, const std::string& b) const { return "ag::rn_div(" + a + ", " + b + ")"; }
+    std::string lit(double v) const { return "((" + W + ")" + hexlit(v) + ")"; }
+    std::string fn(const std::string& name) const {
+        return (L.math == 1 && W == "double") ? "ag::e64::f_" + name : "ag::f_" + name;
+    }
+
+    std::ostringstream& out_for(int id) { return ctx[size_t(id)] ? pro : body; }
+
+    // Declare one variable per component for node `id`.
+    void def(int id, const std::vector<std::string>& exprs, bool is_bool = false) {
+        std::ostringstream& o = out_for(id);
+        std::vector<std::string> names;
+        for (size_t c = 0; c < exprs.size(); ++c) {
+            const std::string nm = "t" + std::to_string(id) + "_" + std::to_string(c);
+            o << "        const " << (is_bool ? "bool" : W) << " " << nm << " = " << exprs[c] << ";\n";
+            names.push_back(nm);
+        }
+        val[size_t(id)] = names;
+    }
+
+    const std::vector<std::string>& emit(int id) {
+        if (done[size_t(id)]) return val[size_t(id)];
+        const Node& n = P.nodes[size_t(id)];
+        for (int k : n.kids) emit(k);
+        auto V = [&](int j) -> const std::vector<std::string>& { return val[size_t(n.kids[size_t(j)])]; };
+        auto K = [&](int j) -> const Node& { return P.nodes[size_t(n.kids[size_t(j)])]; };
+        const std::string& op = n.op;
+        const bool c0 = ctx[size_t(id)] != 0;
+        std::vector<std::string> e;
+        const std::string lane = c0 ? "0" : "l";
+        const std::string gid = c0 ? "g0" : "g";
+
+        if (op == "in") {
+            const bool pbool = n.dtype == DType::U8;
+            for (int c = 0; c < n.comps; ++c) {
+                const std::string src = c0 ? "x" + std::to_string(n.k) + "_0[" + std::to_string(c) + "]"
+                                           : "in" + std::to_string(n.k) + "[" + std::to_string(c) + "][l]";
+                e.push_back(pbool ? "(" + src + " != 0)" : "(" + W + ")" + src);
+            }
+            def(id, e, pbool);
+        } else if (op == "sc") {
+            def(id, {"(" + W + ")a.sc[" + std::to_string(n.k) + "]"});
+        } else if (op == "lit") {
+            def(id, {lit(n.lit)});
+        } else if (op == "bcast") {
+            for (int c = 0; c < n.comps; ++c) e.push_back(V(0)[0]);
+            val[size_t(id)] = e;   // aliases: no new variables
+        } else if (op == "at0") {
+            // Values of the sample-0 subtree are computed in the prologue and
+            // are uniform across lanes.
+            val[size_t(id)] = V(0);
+        } else if (unary_ops().count(op)) {
+            for (int c = 0; c < n.comps; ++c) {
+                const std::string x = V(0)[size_t(c)];
+                if (op == "sq") e.push_back(mul(x, x));
+                else if (op == "neg") e.push_back("(-" + x + ")");
+                else e.push_back(fn(op) + "(" + x + ")");
+            }
+            def(id, e);
+        } else if (binary_ops().count(op)) {
+            for (int c = 0; c < n.comps; ++c) {
+                const std::string a = V(0)[size_t(c)], b = V(1)[size_t(c)];
+                if (op == "add") e.push_back(add(a, b));
+                else if (op == "sub") e.push_back(sub(a, b));
+                else if (op == "mul") e.push_back(mul(a, b));
+                else if (op == "div") e.push_back(div(a, b));
+                else e.push_back(fn(op) + "(" + a + ", " + b + ")");
+            }
+            def(id, e);
+        } else if (op == "scale") {   // CWiseScale: factor * e (expr/nodes/Arithmetic.h:130-140)
+            for (int c = 0; c < n.comps; ++c) e.push_back(mul(V(1)[0], V(0)[size_t(c)]));
+            def(id, e);
+        } else if (op == "mins" || op == "maxs" || op == "pows") {
+            const std::string f = op == "mins" ? "min" : op == "maxs" ? "max" : "pow";
+            for (int c = 0; c < n.comps; ++c) e.push_back(fn(f) + "(" + V(0)[size_t(c)] + ", " + V(1)[0] + ")");
+            def(id, e);
+        } else if (op == "clamp") {   // Elementwise.h:138-167
+            for (int c = 0; c < n.comps; ++c)
+                e.push_back(fn("min") + "(" + fn("max") + "(" + V(0)[size_t(c)] + ", " + V(1)[0] + "), " + V(2)[0] + ")");
+            def(id, e);
+        } else if (cmp_ops().count(op)) {
+            static const std::map<std::string, std::string> sym = {{"gt", ">"}, {"lt", "<"}, {"ge", ">="},
+                                                                   {"le", "<="}, {"eq", "=="}, {"ne", "!="},
+                                                                   {"and", "&&"}, {"or", "||"}};
+            for (int c = 0; c < n.comps; ++c)
+                e.push_back("(" + V(0)[size_t(c)] + " " + sym.at(op) + " " + V(1)[size_t(c)] + ")");
+            def(id, e, true);
+        } else if (op == "not") {
+            for (int c = 0; c < n.comps; ++c) e.push_back("(!" + V(0)[size_t(c)] + ")");
+            def(id, e, true);
+        } else if (op == "select") {   // Elementwise.h:809-846
+            const bool per_sample = K(0).shape.empty();
+            for (int c = 0; c < n.comps; ++c)
+                e.push_back("(" + V(0)[per_sample ? 0 : size_t(c)] + " ? " + V(1)[size_t(c)] + " : " + V(2)[size_t(c)] + ")");
+            def(id, e, n.is_bool);
+        } else if (op == "comp") {
+            val[size_t(id)] = {V(0)[size_t(n.k)]};
+        } else if (op == "seg") {
+            for (int c = 0; c < n.comps; ++c) e.push_back(V(0)[size_t(n.k + c)]);
+            val[size_t(id)] = e;
+        } else if (op == "row" || op == "col") {
+            const int cols = K(0).shape[1];
+            for (int c = 0; c < n.comps; ++c)
+                e.push_back(V(0)[size_t(op == "row" ? n.k * cols + c : c * cols + n.k)]);
+            val[size_t(id)] = e;
+        } else if (op == "transpose") {
+            const int r0 = K(0).shape[0], c0n = K(0).shape[1];
+            for (int r = 0; r < c0n; ++r)
+                for (int c = 0; c < r0; ++c) e.push_back(V(0)[size_t(c * c0n + r)]);
+            val[size_t(id)] = e;
+        } else if (op == "block") {
+            const int cols = K(0).shape[1];
+            for (int r = 0; r < n.ints[2]; ++r)
+                for (int c = 0; c < n.ints[3]; ++c) e.push_back(V(0)[size_t((n.ints[0] + r) * cols + n.ints[1] + c)]);
+            val[size_t(id)] = e;
+        } else if (op == "stack") {
+            for (size_t j = 0; j < n.kids.size(); ++j) e.push_back(V(int(j))[0]);
+            val[size_t(id)] = e;
+        } else if (op == "reshape") {
+            val[size_t(id)] = V(0);
+        } else if (op == "cross") {   // expr/nodes/Geometric.h:55-72
+            const auto& l = V(0);
+            const auto& r = V(1);
+            e = {sub(mul(l[1], r[2]), mul(l[2], r[1])), sub(mul(l[2], r[0]), mul(l[0], r[2])),
+                 sub(mul(l[0], r[1]), mul(l[1], r[0]))};
+            def(id, e);
+        } else if (op == "unit") {   // Geometric.h:99-103 on a per-sample (Item) value
+            const auto& a = V(0);
+            std::string acc = mul(a[0], a[0]);
+            for (size_t c = 1; c < a.size(); ++c) acc = add(mul(a[c], a[c]), acc);
+            const std::string rn = "r" + std::to_string(id);
+            out_for(id) << "        const " << W << " " << rn << " = " << div(lit(1.0), fn("sqrt") + "(" + acc + ")") << ";\n";
+            for (size_t c = 0; c < a.size(); ++c) e.push_back(mul(a[c], rn));
+            def(id, e);
+        } else if (op == "qmul") {   // expr/nodes/Quaternion.h:60-79
+            const auto& l = V(0);
+            const auto& r = V(1);
+            e = {sub(sub(sub(mul(l[0], r[0]), mul(l[1], r[1])), mul(l[2], r[2])), mul(l[3], r[3])),
+                 sub(add(add(mul(l[0], r[1]), mul(l[1], r[0])), mul(l[2], r[3])), mul(l[3], r[2])),
+                 add(add(sub(mul(l[0], r[2]), mul(l[1], r[3])), mul(l[2], r[0])), mul(l[3], r[1])),
+                 add(sub(add(mul(l[0], r[3]), mul(l[1], r[2])), mul(l[2], r[1])), mul(l[3], r[0]))};
+            def(id, e);
+        } else if (op == "qconj") {   // Quaternion.h:103-108
+            const auto& a = V(0);
+            e = {a[0], "(-" + a[1] + ")", "(-" + a[2] + ")", "(-" + a[3] + ")"};
+            def(id, e);
+        } else if (op == "qrot") {   // Quaternion.h:142-168
+            const auto& q = V(0);
+            const auto& v = V(1);
+            const std::string t = "q" + std::to_string(id) + "_";
+            std::ostringstream& o = out_for(id);
+            const std::string two = lit(2.0);
+            o << "        const " << W << " " << t << "x = " << mul(two, sub(mul(q[2], v[2]), mul(q[3], v[1]))) << ";\n";
+            o << "        const " << W << " " << t << "y = " << mul(two, sub(mul(q[3], v[0]), mul(q[1], v[2]))) << ";\n";
+            o << "        const " << W << " " << t << "z = " << mul(two, sub(mul(q[1], v[1]), mul(q[2], v[0]))) << ";\n";
+            e = {add(add(v[0], mul(q[0], t + "x")), sub(mul(q[2], t + "z"), mul(q[3], t + "y"))),
+                 add(add(v[1], mul(q[0], t + "y")), sub(mul(q[3], t + "x"), mul(q[1], t + "z"))),
+                 add(add(v[2], mul(q[0], t + "z")), sub(mul(q[1], t + "y"), mul(q[2], t + "x")))};
+            def(id, e);
+        } else if (op == "pureq") {   // Quaternion.h:192-203
+            const auto& a = V(0);
+            e = {lit(0.0), a[0], a[1], a[2]};
+            def(id, e);
+        } else if (op == "inv" || op == "det") {   // expr/nodes/Inverse.h:73-118, Expression.h:400-428
+            const auto& m = V(0);
+            const int dim = K(0).shape[0];
+            const std::string d = "det" + std::to_string(id);
+            std::ostringstream& o = out_for(id);
+            if (dim == 2) {
+                o << "        const " << W << " " << d << " = " << sub(mul(m[0], m[3]), mul(m[1], m[2])) << ";\n";
+                if (op == "det") e = {d};
+                else e = {div(m[3], d), div("(-" + m[1] + ")", d), div("(-" + m[2] + ")", d), div(m[0], d)};
+            } else {
+                const std::string &a = m[0], &b = m[1], &c = m[2], &dd = m[3], &ee = m[4], &f = m[5], &g = m[6],
+                                  &h = m[7], &k = m[8];
+                o << "        const " << W << " " << d << " = "
+                  << add(sub(mul(a, sub(mul(ee, k), mul(f, h))), mul(b, sub(mul(dd, k), mul(f, g)))),
+                         mul(c, sub(mul(dd, h), mul(ee, g))))
+                  << ";\n";
+                if (op == "det") {
+                    e = {d};
+                } else {
+                    e = {div(sub(mul(ee, k), mul(f, h)), d), div(sub(mul(c, h), mul(b, k)), d),
+                         div(sub(mul(b, f), mul(c, ee)), d), div(sub(mul(f, g), mul(dd, k)), d),
+                         div(sub(mul(a, k), mul(c, g)), d), div(sub(mul(c, dd), mul(a, f)), d),
+                         div(sub(mul(dd, h), mul(ee, g)), d), div(sub(mul(b, g), mul(a, h)), d),
+                         div(sub(mul(a, ee), mul(b, dd)), d)};
+                }
+            }
+            def(id, e);
+        } else if (op == "trace") {   // Expression.h:381-398
+            const auto& m = V(0);
+            const int dim = K(0).shape[0];
+            std::string t = add(m[0], m[size_t(dim + 1)]);
+            if (dim == 3) t = add(t, m[8]);
+            def(id, {t});
+        } else if (op == "matvec" || op == "matmul" || op == "outer") {
+            const auto& a = V(0);
+            const auto& b = V(1);
+            const auto& sa = K(0).shape;
+            const auto& sb = K(1).shape;
+            if (op == "outer") {
+                for (int i = 0; i < sa[0]; ++i)
+                    for (int j = 0; j < sb[0]; ++j) e.push_back(mul(a[size_t(i)], b[size_t(j)]));
+            } else if (op == "matvec") {
+                for (int i = 0; i < sa[0]; ++i) {
+                    std::string acc = mul(a[size_t(i * sa[1])], b[0]);
+                    for (int k = 1; k < sa[1]; ++k) acc = add(mul(a[size_t(i * sa[1] + k)], b[size_t(k)]), acc);
+                    e.push_back(acc);
+                }
+            } else {
+                for (int i = 0; i < sa[0]; ++i)
+                    for (int j = 0; j < sb[1]; ++j) {
+                        std::string acc = mul(a[size_t(i * sa[1])], b[size_t(j)]);
+                        for (int k = 1; k < sa[1]; ++k)
+                            acc = add(mul(a[size_t(i * sa[1] + k)], b[size_t(k * sb[1] + j)]), acc);
+                        e.push_back(acc);
+                    }
+            }
+            def(id, e);
+        } else if (op == "dot" || op == "sqnorm" || op == "norm" || op == "rnorm" || op == "sum" || op == "maxnorm") {
+            // expr/Reduce.h:149-188: acc = f(x0); acc = Reduce(f(x_{k+1}), acc)
+            const auto& a = V(0);
+            const int m = K(0).comps;
+            auto term = [&](int c) -> std::string {
+                if (op == "dot") return mul(a[size_t(c)], V(1)[size_t(c)]);
+                if (op == "sum") return a[size_t(c)];
+                if (op == "maxnorm") return fn("abs") + "(" + a[size_t(c)] + ")";
+                return mul(a[size_t(c)], a[size_t(c)]);
+            };
+            std::string acc = term(0);
+            for (int c = 1; c < m; ++c) {
+                const std::string t = term(c);
+                acc = op == "maxnorm" ? "((" + t + ") > (" + acc + ") ? (" + t + ") : (" + acc + "))" : add(t, acc);
+            }
+            if (op == "norm") acc = fn("sqrt") + "(" + acc + ")";
+            if (op == "rnorm") acc = div(lit(1.0), fn("sqrt") + "(" + acc + ")");
+            def(id, {acc});
+        } else if (op == "uniform" || op == "normal" || op == "lognormal" || op == "exponential" || op == "bernoulli") {
+            const std::string key = "a.key[" + std::to_string(n.k) + "]";
+            const bool b0 = K(0).shape.empty();
+            const bool b1 = n.kids.size() > 1 && K(1).shape.empty();
+            const std::string wp = "(" + W + "*)0";
+            for (int c = 0; c < n.comps; ++c) {
+                const std::string x0 = V(0)[b0 ? 0 : size_t(c)];
+                const std::string x1 = n.kids.size() > 1 ? V(1)[b1 ? 0 : size_t(c)] : "";
+                const std::string cc = std::to_string(c) + "u";
+                if (op == "uniform") {   // DistributionLeaf.h:125-131
+                    e.push_back(add(x0, mul(sub(x1, x0), "ag::draw01(" + wp + ", " + key + " ^ AG_SALT_UNIFORM, " + gid + ", " + cc + ")")));
+                } else if (op == "normal") {   // DistributionLeaf.h:192-199
+                    e.push_back(add(x0, mul(x1, "ag::drawn(" + wp + ", " + key + " ^ AG_SALT_NORMAL, " + gid + ", " + cc + ")")));
+                } else if (op == "lognormal") {   // DistributionLeaf.h:257-264
+                    e.push_back(fn("exp") + "(" + add(x0, mul(x1, "ag::drawn(" + wp + ", " + key + " ^ AG_SALT_LOGNORMAL, " + gid + ", " + cc + ")")) + ")");
+                } else if (op == "exponential") {   // DistributionLeaf.h:329-333
+                    e.push_back(div("(-" + fn("log") + "(ag::draw01(" + wp + ", " + key + " ^ AG_SALT_EXPONENTIAL, " + gid + ", " + cc + ")))", x0));
+                } else {   // DistributionLeaf.h:380-385
+                    e.push_back("(ag::draw01(" + wp + ", " + key + " ^ AG_SALT_BERNOULLI, " + gid + ", " + cc + ") < " + x0 + " ? " + lit(1.0) + " : " + lit(0.0) + ")");
+                }
+            }
+            def(id, e);
+        } else {
+            fail("no generator for '" + op + "'");
+        }
+        (void)lane;
+        done[size_t(id)] = 1;
+        return val[size_t(id)];
+    }
+};
+
+std::string ctype(DType d) {
+    switch (d) {
+    case DType::F64: return "double";
+    case DType::F32: return "float";
+    case DType::FF: return "float";
+    case DType::I32: return "int";
+    case DType::U8: return "unsigned char";
+    }
+    return "double";
+}
+
+}  // namespace
+
+Plan parse_plan(const std::string& text) {
+    Parser ps(text.c_str());
+    return ps.run();
+}
+
+int effective_vec(const Plan& plan, const Lowering& low) {
+    if (low.vec > 0) return low.vec;
+    int widest = dtype_size(plan.dst_dtype);
+    for (DType d : plan.operand_dtype) widest = std::max(widest, dtype_size(d));
+    return widest >= 8 ? 2 : 4;
+}
+
+std::string generate_source(const Plan& plan_in, const Lowering& low) {
+    // Re-derive the sample contexts (at0 subtrees) from the node graph: every
+    // node reachable only through `at0` belongs to the sample-0 prologue.
+    const Plan& P = plan_in;
+    std::vector<int> ctx(P.nodes.size(), 1);
+    {
+        std::vector<int> stack = {P.root};
+        std::vector<char> seen(P.nodes.size(), 0);
+        while (!stack.empty()) {
+            const int id = stack.back();
+            stack.pop_back();
+            if (seen[size_t(id)]) continue;
+            seen[size_t(id)] = 1;
+            ctx[size_t(id)] = 0;
+            if (P.nodes[size_t(id)].op == "at0") continue;
+            for (int k : P.nodes[size_t(id)].kids) stack.push_back(k);
+        }
+        // A node used both inside and outside at0 would need two copies; the
+        // parser keys its memo by context, so such nodes are already distinct.
+    }
+    Gen g(P, low, ctx);
+    const std::vector<std::string>& root = g.emit(P.root);
+
+    const int vec = effective_vec(P, low);
+    std::ostringstream o;
+    o << "// generated by aether_gb300 from an aether-ir/1 plan\n";
+    o << "#include \"ag_device.cuh\"\n";
+    if (low.math == 1) o << "#include \"ag_emu64.cuh\"\n";
+    o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
+    const std::string W = g.W, S = g.S;
+    const bool sum = P.wants_sum(), store = P.wants_store();
+    const bool rw = P.op == "add" || P.op == "sub";
+
+    // The chunk body: one pass of a CTA over block*ipt*VEC consecutive samples.
+    o << "template <int VEC>\n__device__ __forceinline__ void ag_chunk(const AgArgs& a, ag_u64 chunk";
+    if (sum) o << ", double& acc_h, double& acc_c";
+    o << ") {\n";
+    o << "    constexpr int L = AG_IPT * VEC;\n";
+    o << "    ag_u64 s0[AG_IPT];\n";
+    o << "#pragma unroll\n    for (int j = 0; j < AG_IPT; ++j) s0[j] = chunk * (ag_u64)(AG_BLOCK * AG_IPT * VEC) + ((ag_u64)j * AG_BLOCK + threadIdx.x) * VEC;\n";
+    // Loads of every operand used in the lane context.
+    std::set<int> lane_ops, zero_ops;
+    for (size_t id = 0; id < P.nodes.size(); ++id) {
+        const Node& n = P.nodes[id];
+        if (n.op != "in") continue;
+        if (!g.done[id]) continue;
+        (ctx[id] ? zero_ops : lane_ops).insert(n.k);
+    }
+    for (int k : lane_ops) {
+        const std::string T = ctype(P.operand_dtype[size_t(k)]);
+        const int C = P.operand_comps[size_t(k)];
+        o << "    const " << T << "* __restrict__ p" << k << " = (const " << T << "*)a.ops[" << k << "];\n";
+        o << "    " << T << " in" << k << "[" << C << "][L];\n";
+        o << "#pragma unroll\n    for (int c = 0; c < " << C << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, "
+          << T << ">::load(p" << k << " + c * a.pitch[" << k << "], s0[j], a.n, &in" << k << "[c][j * VEC]);\n";
+    }
+    if (rw) {
+        o << "    " << S << "* __restrict__ pd = (" << S << "*)a.dst;\n";
+        o << "    " << S << " cur[" << P.dst_comps << "][L];\n";
+        o << "#pragma unroll\n    for (int c = 0; c < " << P.dst_comps << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, "
+          << S << ">::load_rw(pd + c * a.dst_pitch, s0[j], a.n, &cur[c][j * VEC]);\n";
+    }
+    // Sample-0 prologue (at0 subtrees): loads of sample 0 and their values.
+    for (int k : zero_ops) {
+        const std::string T = ctype(P.operand_dtype[size_t(k)]);
+        const int C = P.operand_comps[size_t(k)];
+        o << "    " << T << " x" << k << "_0[" << C << "];\n";
+        o << "#pragma unroll\n    for (int c = 0; c < " << C << "; ++c) x" << k << "_0[c] = ((const " << T << "*)a.ops[" << k
+          << "])[c * a.pitch[" << k << "]];\n";
+    }
+    if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n";
+    o << g.pro.str();
+    if (store) o << "    " << S << " out[" << P.dst_comps << "][L];\n";
+    o << "#pragma unroll\n    for (int l = 0; l < L; ++l) {\n";
+    if (P.has_random) o << "        const ag_u32 g = a.offset + (ag_u32)(s0[l / VEC] + (ag_u64)(l % VEC));\n";
+    o << g.body.str();
+    for (int c = 0; c < P.dst_comps; ++c) {
+        const std::string v = root[size_t(c)];
+        if (store) {
+            if (P.op == "set" || P.op == "setsum") o << "        out[" << c << "][l] = (" << S << ")" << v << ";\n";
+            else if (P.op == "add") o << "        out[" << c << "][l] = (" << S << ")ag::rn_add((" << W << ")cur[" << c << "][l], " << v << ");\n";
+            else o << "        out[" << c << "][l] = (" << S << ")ag::rn_sub((" << W << ")cur[" << c << "][l], " << v << ");\n";
+        }
+    }
+    if (sum) {
+        o << "        if (s0[l / VEC] + (ag_u64)(l % VEC) < a.n) ag::neumaier_add(acc_h, acc_c, (double)(" << root[0] << "));\n";
+    }
+    o << "    }\n";
+    if (store) {
+        o << "    " << S << "* __restrict__ po = (" << S << "*)a.dst;\n";
+        o << "#pragma unroll\n    for (int c = 0; c < " << P.dst_comps << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, " << S
+          << ">::store(po + c * a.dst_pitch, s0[j], a.n, &out[c][j * VEC]);\n";
+    }
+    o << "}\n";
+
+    std::ostringstream k;
+    k << o.str();
+    const std::string lb = low.min_blocks > 0 ? "__launch_bounds__(AG_BLOCK, " + std::to_string(low.min_blocks) + ")"
+                                              : "__launch_bounds__(AG_BLOCK)";
+    for (int variant = 0; variant < 2; ++variant) {
+        const std::string name = variant == 0 ? "ag_plan_v" : "ag_plan_s";
+        const std::string V = variant == 0 ? "AG_VEC" : "1";
+        k << "extern \"C\" __global__ void " << lb << " " << name << "(const AgArgs a) {\n";
+        k << "    const ag_u64 per = (ag_u64)AG_BLOCK * AG_IPT * " << V << ";\n";
+        k << "    const ag_u64 nchunks = (a.n + per - 1) / per;\n";
+        k << "    for (ag_u64 ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {\n";
+        if (sum) {
+            k << "        double h = 0.0, c = 0.0;\n";
+            k << "        ag_chunk<" << V << ">(a, ch, h, c);\n";
+            k << "        ag::sum_chunk_finish<AG_BLOCK>(a, ch, nchunks, h, c);\n";
+        } else {
+            k << "        ag_chunk<" << V << ">(a, ch);\n";
+        }
+        k << "    }\n}\n";
+    }
+    return k.str();
+}
+
+}  // namespace ag

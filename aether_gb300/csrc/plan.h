@@ -1,0 +1,68 @@
+// plan.h -- the aether-ir/1 plan: parser, type checker and CUDA code generator.
+//
+// A plan is one fused assignment `dst <op>= expr` over the sample axis of SoA
+// arrays, the statement a consumer of the reference writes inside its own
+// kernel (`d[i] = a + b*exp(c)`, expr/Assign.h:251-346). The tree's text is its
+// type signature; the generated kernel is cached by the hash of that text and
+// the lowering options.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ag {
+
+enum class DType { F64, F32, FF, I32, U8 };
+
+struct Node {
+    std::string op;
+    std::vector<int> kids;
+    std::vector<int> shape;   // element extents, row-major; empty = rank 0
+    int comps = 1;
+    bool is_bool = false;
+    int k = 0;                // operand / scalar / key slot, or the first integer argument
+    std::vector<int> ints;    // further integer arguments
+    double lit = 0.0;
+    DType dtype = DType::F64; // storage type of an `in` leaf
+};
+
+struct Plan {
+    DType dst_dtype = DType::F64;
+    std::vector<int> dst_shape;
+    int dst_comps = 1;
+    std::string op;           // set | add | sub | sum | setsum
+    std::vector<Node> nodes;  // topological: every kid precedes its parent
+    int root = -1;
+    int n_operands = 0;       // 1 + highest operand slot used
+    int n_scalars = 0;
+    int n_keys = 0;
+    std::vector<DType> operand_dtype;
+    std::vector<int> operand_comps;
+    bool has_random = false;
+    bool wants_sum() const { return op == "sum" || op == "setsum"; }
+    bool wants_store() const { return op != "sum"; }
+};
+
+// Lowering options (part of the cache key).
+struct Lowering {
+    int block = 256;          // threads per CTA
+    int ipt = 1;              // lane groups per thread per chunk
+    int vec = 0;              // samples per lane group (0 = 16 bytes of the widest storage type)
+    bool contract = true;     // allow FMA contraction of arithmetic nodes
+    int math = 0;             // 0 = native FP64 pipe, 1 = emulated FP64 on FP32/INT pipes
+    int min_blocks = 0;       // __launch_bounds__ second argument (0 = none)
+};
+
+Plan parse_plan(const std::string& text);
+const char* dtype_name(DType d);
+int dtype_size(DType d);
+
+// Generated CUDA source for the plan: kernels `ag_plan_v` (vectorized lane
+// groups) and `ag_plan_s` (one sample per lane group).
+std::string generate_source(const Plan& plan, const Lowering& low);
+
+// Chunk = samples one CTA covers per pass = block * ipt * vec.
+int effective_vec(const Plan& plan, const Lowering& low);
+
+}  // namespace ag

@@ -1,0 +1,319 @@
+"""Benchmark of the fused SoA expression path (large streaming FP64 workload).
+
+One step = the two kernels of the large streaming FP64 workload:
+  (a) d = sqrt(a*a+b*b) * log1p(|c|) + rsqrt(1 + d0*d0) over four
+      Array<double,3> inputs of 2^26 samples (uniform[-4,4) from Philox seed 7,
+      substreams 0..3), one Array<double,3> output: 120 B/sample;
+  (b) an in-place Philox normal fill (Box-Muller) of 2^28 doubles (substream 4
+      of seed 7): 8 B/sample, write only.
+value = algorithmic bytes of both kernels / device time (inputs resident in
+HBM, CUDA events on the launching stream). Inputs are larger than L2, so no
+flush runs between steps. e2e = the same step through the C-ABI with pinned
+host buffers: host->device copies of the four inputs and device->host copies
+of both outputs inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "fused SoA expr HBM GB/s (% of peak); served samples/s, p50/p99 vs plain launch"
+UNIT = "GB/s"
+N_EXPR = 1 << 26          # samples of the expression kernel
+N_FILL = 1 << 28          # doubles of the normal fill
+BYTES_EXPR = N_EXPR * 120
+BYTES_FILL = N_FILL * 8
+WORKLOAD = ("large streaming FP64: 4 x Array<double,3> of 2^26 samples -> "
+            "sqrt(a*a+b*b)*log1p(|c|)+rsqrt(1+d0*d0); + Philox normal fill of 2^28 doubles")
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per sample of the expression kernel from the committed ncu
+    summary (profiles/), or None."""
+    path = os.path.join(REPO, "profiles", "ncu_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("expr_bytes_per_sample:"):
+                return float(line.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_leg(steps, warmup, nthreads=0, expr_samples=1 << 23, fill_samples=1 << 25):
+    """The reference's CPU algorithm (OpenMP user loop, oracle/ restatement)
+    on a bounded sample of the same workload. Returns (GB/s, seconds/step)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import numpy as np
+    import pyoracle as po
+    nt = nthreads or po.max_threads()
+    n = expr_samples
+    k7 = po.generator_key(7)
+    ins = [po.fill_uniform_f64(po.substream_key(k7, s), -4.0, 4.0, 3, n, nthreads=nt) for s in range(4)]
+    key_fill = po.substream_key(k7, 4)
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        po.cfg2a(*ins, nthreads=nt)
+        po.fill_normal_f64(key_fill, 0.0, 1.0, 1, fill_samples, nthreads=nt)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+    t = statistics.median(times)
+    gbs = (n * 120 + fill_samples * 8) / t / 1e9
+    sample = ("expression on %d samples (2^%d) + normal fill of %d doubles (2^%d) per step, median of %d"
+              % (n, n.bit_length() - 1, fill_samples, fill_samples.bit_length() - 1, len(times)))
+    return gbs, t, nt, sample
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    gbs, t, nt, sample = cpu_leg(args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox seed 7)",
+        "config": {"workload": WORKLOAD, "sample": sample, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
+        "e2e": {"value": round(gbs, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import aether_gb300 as ag
+
+    math_mode = args.math
+    stream = torch.cuda.current_stream()
+    g = ag.Generator(7)
+    arrs = [ag.Array("f64", (3,), N_EXPR) for _ in range(4)]
+    for k, a in enumerate(arrs):
+        ag.assign(a, g.substream(k).uniform(3, -4.0, 4.0))
+    d = ag.Array("f64", (3,), N_EXPR)
+    z = ag.Array("f64", (1,), N_FILL)
+    a, b, c, d0 = (x.view() for x in arrs)
+    expr = ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c)) + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0)
+    k_expr = ag.prepare(d, expr, math=math_mode)
+    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=math_mode)
+    torch.cuda.synchronize()
+
+    def step():
+        k_expr()
+        k_fill()
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            k_expr()
+            ev[i][1].record(stream)
+            k_fill()
+            ev[i][2].record(stream)
+        end.record(stream)
+        torch.cuda.synchronize()
+    total_ms = start.elapsed_time(end)
+    t_expr = [e[0].elapsed_time(e[1]) for e in ev]
+    t_fill = [e[1].elapsed_time(e[2]) for e in ev]
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = ws * (BYTES_EXPR + BYTES_FILL) / (ms_step * 1e-3) / 1e9
+
+    # e2e through the C-ABI: pinned host buffers, copies inside the timed region.
+    e2e = None
+    if not args.no_e2e:
+        L = ag._abi.lib()
+        import ctypes
+        nb = N_EXPR * 3 * 8
+        host_in = [torch.empty((3, N_EXPR), dtype=torch.float64, pin_memory=True) for _ in range(4)]
+        for h, x in zip(host_in, arrs):
+            h.copy_(x.data[:, :N_EXPR])
+        host_out = torch.empty((3, N_EXPR), dtype=torch.float64, pin_memory=True)
+        host_fill = torch.empty((1, N_FILL), dtype=torch.float64, pin_memory=True)
+        s = ctypes.c_void_p(stream.cuda_stream)
+
+        def e2e_step():
+            for h, x in zip(host_in, arrs):
+                ag._abi.check(L.aether_copy(1, local, ctypes.c_void_p(x.data.data_ptr()), 2, 0,
+                                            ctypes.c_void_p(h.data_ptr()), nb, s))
+            k_expr()
+            k_fill()
+            ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_out.data_ptr()), 1, local,
+                                        ctypes.c_void_p(d.data.data_ptr()), nb, s))
+            ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_fill.data_ptr()), 1, local,
+                                        ctypes.c_void_p(z.data.data_ptr()), N_FILL * 8, s))
+            ag._abi.check(L.aether_stream_sync(local, s))
+
+        e2e_step()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e_steps = max(2, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            e2e_step()
+        e_ms = (time.perf_counter() - t0) * 1e3 / e_steps
+        if dist:
+            t = torch.tensor([e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        e2e = {"value": round(ws * (BYTES_EXPR + BYTES_FILL) / (e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = peaks()
+    te = statistics.mean(t_expr)
+    tf = statistics.mean(t_fill)
+    achieved = BYTES_EXPR / (te * 1e-3) / 1e9
+    tr = profile_traffic()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": round(tr * N_EXPR) if tr else None,
+                "kernel": "expression (a) sqrt/log1p/rsqrt plan", "kernel_ms": round(te, 4),
+                "fill_ms": round(tf, 4), "fill_gbs": round(BYTES_FILL / (tf * 1e-3) / 1e9, 2),
+                "fill_frac": round(BYTES_FILL / (tf * 1e-3) / 1e9 / peak, 4)}
+    cpu = None
+    if not args.no_cpu:
+        gbs, t, nt, sample = cpu_leg(1, 1)
+        cpu = {"value": round(gbs, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 seed 7, generated on device)",
+        "config": {"workload": WORKLOAD, "samples_expr": N_EXPR, "samples_fill": N_FILL,
+                   "l2": "inputs larger than L2 (no flush)", "math": ["native FP64", "emulated FP64"][math_mode],
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--math", type=int, default=0, help="0 native FP64, 1 emulated FP64")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,143 @@
+/*
+ * aether_gb300.h -- the C-ABI boundary of the GB300 fused-expression engine.
+ *
+ * Plain C: pointers, sizes and status codes only. Every entry point returns 0
+ * on success, 1 on failure (the message is in aether_last_error(), kept per
+ * thread) and 2 when an optional feature is missing, the convention of the
+ * reference's plugin seam (dsc/src/seam.h:16-53, dsc/src/plugin.cpp:22-39).
+ * Nothing throws across this boundary. Streams are raw cudaStream_t values
+ * passed as void*; NULL is the legacy default stream.
+ *
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef AETHER_GB300_H
+#define AETHER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AETHER_GB300_ABI 1
+
+enum { AETHER_OK = 0, AETHER_FAIL = 1, AETHER_MISSING = 2 };
+/* Memory kinds, as in the reference seam (dsc/src/seam.h:10). */
+enum { AETHER_MEM_CPU = 0, AETHER_MEM_DEVICE = 1, AETHER_MEM_PINNED = 2 };
+
+/* ------------------------------------------------------------------------- *
+ * Memory. Replaces the AetherMemoryV1 table of dsc/src/seam.h:22-53
+ * (probe, runtime_version, last_error, chunk_alloc, chunk_release, drain,
+ * fill, copy, stream_wait, stream_sync), backed on the reference side by
+ * aether/chunk/Chunk.h:111-260 and aether/chunk/Copy.h:87-192.
+ * ------------------------------------------------------------------------- */
+
+/* dsc/src/seam.h:24 probe: 0 only if a driver answers and >= 1 device exists. */
+int aether_probe(int* device_count);
+/* dsc/src/seam.h:25 runtime_version. */
+int aether_runtime_version(int* version);
+/* dsc/src/seam.h:27 last_error: the calling thread's last failure message. */
+const char* aether_last_error(void);
+/* dsc/src/seam.h:28 chunk_alloc: `bytes` of `kind` memory on `dev`; device
+ * memory is stream-ordered on `stream` (chunk/Chunk.h:217-260). */
+int aether_chunk_alloc(int kind, int dev, size_t bytes, void* stream, void** chunk, void** ptr);
+/* dsc/src/seam.h:29 chunk_release: frees on the chunk's stream; deferred while
+ * that stream is capturing (chunk/StreamOrdered.h:141-286). */
+void aether_chunk_release(void* chunk);
+/* dsc/src/seam.h:30 drain: release deferred frees whose capture has ended. */
+void aether_drain(void);
+/* dsc/src/seam.h:31 fill: repeat the `width`-byte `value` over `bytes`
+ * (chunk/Fill.h:33). */
+int aether_fill(int kind, int dev, void* ptr, size_t bytes, const void* value, size_t width, void* stream);
+/* dsc/src/seam.h:32 copy: any legal (dst kind, src kind) pair, stream-ordered
+ * (chunk/Copy.h:87-192). */
+int aether_copy(int dst_kind, int dst_dev, void* dst, int src_kind, int src_dev, const void* src, size_t bytes,
+                void* stream);
+/* dsc/src/seam.h:34 stream_wait: `consumer` waits for work queued on `producer`. */
+int aether_stream_wait(int dev, void* producer, void* consumer);
+/* dsc/src/seam.h:35 stream_sync. */
+int aether_stream_sync(int dev, void* stream);
+
+/* ------------------------------------------------------------------------- *
+ * Plans: one fused assignment `dst <op>= expr` lowered to one sm_103a kernel.
+ * Replaces the consumer-written __global__ that evaluates `view[i] = expr`
+ * (expr/Assign.h:191-231 RecursiveAssign/SampleRef, view/View.h:385-418) and
+ * its launch (backend/cuda/Launch.h:53-74 launchConfig, :84-88
+ * checkLastLaunch), and the bundle variant (backend/cuda/bundle/Assign.h:55-268,
+ * bundle/LoadStore.h:149-318). The expression is the aether-ir/1 text that
+ * the C++ front end (aether_gb300/include/aether) serialises from the
+ * expression tree's type; the kernel is compiled once per (text, lowering)
+ * and cached in memory and on disk by hash.
+ * ------------------------------------------------------------------------- */
+
+/* One SoA operand: plane c of the array starts at ptr + c * pitch elements
+ * (array/Array.h:288-304: pitch = capacity, a multiple of 32 samples). */
+typedef struct AetherOperand {
+    const void* ptr;
+    uint64_t pitch;
+} AetherOperand;
+
+typedef struct AetherLaunch {
+    uint64_t n;                   /* samples to evaluate */
+    uint32_t sample_offset;       /* global sample id of sample 0 (SampleIndex::global) */
+    uint32_t flags;               /* 0 */
+    void* dst;                    /* destination planes (device memory) */
+    uint64_t dst_pitch;           /* elements between destination planes */
+    const AetherOperand* operands;
+    uint32_t n_operands;
+    const double* scalars;        /* runtime scalars (host memory), e.g. CWiseScale factors */
+    uint32_t n_scalars;
+    const uint64_t* keys;         /* Generator keys of random leaves (random/Generator.h:183) */
+    uint32_t n_keys;
+    double* reduce_out;           /* sum plans: device pointer to (hi, comp) */
+    void* workspace;              /* sum plans: device scratch, or NULL for the plan's own */
+    uint64_t workspace_bytes;
+} AetherLaunch;
+
+/* Lowering options; any field <= 0 takes the tuned default. */
+typedef struct AetherLowering {
+    int block;        /* threads per CTA */
+    int ipt;          /* lane groups per thread per chunk */
+    int vec;          /* samples per lane group (vector width) */
+    int contract;     /* 1: FMA contraction allowed, 0: every add/mul rounds (-fmad=false), -1: default (1) */
+    int math;         /* 0: FP64 on the FP64 pipe; 1: FP64 emulated on the FP32/INT pipes */
+    int min_blocks;   /* __launch_bounds__ min blocks per SM */
+} AetherLowering;
+
+typedef struct AetherPlanInfo {
+    uint64_t hash;            /* cache key of the compiled kernel */
+    int n_operands, n_scalars, n_keys;
+    int dst_comps;
+    int dst_dtype;            /* 0 f64, 1 f32, 2 ff */
+    int is_sum;               /* writes a (hi, comp) global sum */
+    int block, ipt, vec;
+    int registers;            /* per thread, of the vectorized kernel */
+    int blocks_per_sm;        /* occupancy of the vectorized kernel */
+    double compile_ms;        /* 0 when the kernel came from a cache */
+} AetherPlanInfo;
+
+/* Parse, check and compile `ir` (aether-ir/1). `lowering` may be NULL. */
+int aether_plan_create(const char* ir, const AetherLowering* lowering, void** plan);
+int aether_plan_info(void* plan, AetherPlanInfo* info);
+/* Device scratch a sum plan needs for `n` samples (0 for other plans). */
+int aether_plan_workspace_size(void* plan, uint64_t n, uint64_t* bytes);
+/* Enqueue the plan on `stream`. Never synchronises. */
+int aether_plan_launch(void* plan, const AetherLaunch* args, void* stream);
+/* The generated CUDA source (for inspection); `len` receives its length. */
+int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len);
+void aether_plan_release(void* plan);
+
+/* Offline lowering, no device needed: parse and check `ir`, write the CUDA
+ * source of its kernel into `buf` (up to `cap` bytes, NUL-terminated) and its
+ * length into `len`. Stands in for the reference's compile-time type check of
+ * an expression (the static_asserts of expr/nodes/*.h and expr/Assign.h:205-231). */
+int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* buf, size_t cap, size_t* len);
+/* Compile `source` with NVRTC for `arch` (e.g. "sm_103a") without loading it;
+ * on failure the compiler log is the last error. */
+int aether_nvrtc_check(const char* source, const char* arch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

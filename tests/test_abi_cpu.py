@@ -1,0 +1,126 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol that
+include/*.h declares, and its offline lowering checks and compiles plans
+(NVRTC cross-compiles for sm_103a without a device)."""
+
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import REPO
+
+
+def _declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(aether_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    from aether_gb300 import _abi
+    L = _abi.lib()
+    declared = _declared_symbols()
+    assert len(declared) >= 15
+    for name in sorted(declared):
+        assert hasattr(L, name), "libaether_gb300.so does not export " + name
+    # The Python binding covers every declared symbol too.
+    assert declared <= set(_abi._SIGS), declared - set(_abi._SIGS)
+
+
+def test_only_aether_symbols_are_exported():
+    import subprocess
+    from aether_gb300 import _abi
+    _abi.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", _abi.LIB_PATH], capture_output=True, text=True).stdout
+    funcs = [l.split()[-1] for l in out.splitlines() if " T " in l]
+    assert funcs and all(f.startswith("aether_") for f in funcs), funcs
+
+
+def test_probe_without_device_fails_cleanly():
+    import torch
+    from aether_gb300 import _abi
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    n = ctypes.c_int(0)
+    assert _abi.lib().aether_probe(ctypes.byref(n)) == 1
+    assert _abi.lib().aether_last_error()
+
+
+import aether_gb300 as ag
+from aether_gb300 import _abi
+from aether_gb300.expr import IrContext, Operand, plan_text
+
+
+def _leaf(k, shape=(3,), dt="f64"):
+    return Operand(0x10000 * (k + 1), 1024, dt, shape)
+
+
+def _corpus():
+    a, b, c, d0 = (_leaf(k) for k in range(4))
+    q, p = _leaf(4, (4,)), _leaf(5, (4,))
+    M = _leaf(6, (3, 3))
+    x, y = _leaf(7, (8,), "f32"), _leaf(8, (8,), "f32")
+    g = ag.Generator(7)
+    yield "cfg1", "f64", (3,), "set", a + b * c + ag.cwiseSin(a) * ag.cwiseExp((c * c) * (-1.0))
+    yield "cfg2a", "f64", (3,), "set", (ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c))
+                                       + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0))
+    yield "normal", "f64", (1,), "set", g.substream(4).normal(1, 0.0, 1.0)
+    yield "uniform", "f64", (3,), "set", g.substream(0).uniform(3, -4.0, 4.0)
+    yield "cross", "f64", (3,), "set", a.cross(b)
+    yield "qrot", "f64", (3,), "set", q.quatRotate(a)
+    yield "qmul", "f64", (4,), "set", q.quatMul(p)
+    yield "inv_guard", "f64", (3, 3), "set", ag.select(ag.cwiseAbs(M.det()) > 1e-300, M.inverse(),
+                                                       ag.constant(0.0, (3, 3)))
+    yield "dot_sum_f32", "f32", (), "setsum", x.dot(y)
+    yield "sum_f64", "f64", (), "sum", a.dot(b)
+    yield "accumulate", "f64", (3,), "add", a * 2.0
+    yield "unit_view", "f64", (3,), "set", a * a.rNorm().at_sample0()
+    yield "matmul", "f64", (3, 3), "set", M.matmul(M.transpose())
+    yield "lognormal_f32", "f32", (2,), "set", g.lognormal(2, 0.1, 0.5)
+    yield "clamp_pow", "f64", (3,), "set", ag.clamp(ag.cwisePow(ag.cwiseAbs(a), 1.5), -2.0, 2.0)
+
+
+@pytest.mark.parametrize("case", list(_corpus()), ids=lambda c: c[0])
+@pytest.mark.parametrize("contract", [0, 1])
+def test_corpus_lowers_and_compiles_for_sm103a(case, contract):
+    name, dt, shape, op, e = case
+    ir = plan_text(dt, shape, op, e, IrContext())
+    src = _abi.generate(ir, _abi.lowering(contract=contract))
+    assert "ag_plan_v" in src and "ag_plan_s" in src
+    _abi.nvrtc_check(src, "sm_103a")
+
+
+@pytest.mark.parametrize("bad, msg", [
+    ("(plan f64 [3] set (add (in 0 f64 [3]) (in 1 f64 [2])))", "shapes differ"),
+    ("(plan f64 [2] set (in 0 f64 [3]))", "does not match"),
+    ("(plan f64 [3] set (frob (in 0 f64 [3])))", "unknown node"),
+    ("(plan f64 [3] set (in 0 f64 [3])", "unexpected end"),
+    ("(plan f64 [3] set (cross (in 0 f64 [4]) (in 1 f64 [4])))", "cross"),
+    ("(plan f64 [] sum (in 0 f64 [3]))", "does not match"),
+    ("(plan f64 [3] set (in 1 f64 [3]))", "unused"),
+    ("(plan f64 [3] set (select (in 0 f64 [3]) (in 0 f64 [3]) (in 0 f64 [3])))", "boolean"),
+    ("(plan q64 [3] set (in 0 f64 [3]))", "dtype"),
+])
+def test_bad_plans_are_rejected_with_a_message(bad, msg):
+    with pytest.raises(ag.AetherError, match=msg):
+        _abi.generate(bad)
+
+
+def test_structural_cse_shares_subtrees():
+    a = _leaf(0)
+    e = ag.cwiseSin(a) * ag.cwiseSin(a)
+    src = _abi.generate(plan_text("f64", (3,), "set", e, IrContext()))
+    assert src.count("ag::f_sin(") == 3   # once per component, not twice
+
+
+def test_emulated_math_requires_f64_plan():
+    a = _leaf(0, (3,), "f32")
+    ir = plan_text("f32", (3,), "set", a + a, IrContext())
+    src = _abi.generate(ir, _abi.lowering(math=1))
+    assert "ag_emu64" in src

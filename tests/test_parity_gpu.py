@@ -1,0 +1,419 @@
+"""GPU parity: every plan kernel against the oracle (the reference's CPU
+algorithm restated in oracle/), on the same seeded inputs.
+
+Bounds: Philox bits and uniforms, index work, and arithmetic/geometry nodes
+lowered with contraction off are bit-exact. Transcendental nodes are held to
+the CUDA Math API's documented double-precision maximum error plus glibc's
+own (1 ulp), measured in ulps of the largest term of the expression where a
+sum can cancel. Box-Muller normals use the reference's TIER-TOL band
+(abs+rel 1e-12 double, 1e-5 float: random/detail/Backend.h:44-51)."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import assert_ulp, ulp_diff
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+
+
+import aether_gb300 as ag
+
+ULP_F64 = {"exp": 2, "log": 2, "log1p": 2, "expm1": 2, "sin": 3, "cos": 3, "tan": 3, "asin": 3, "acos": 3,
+           "atan": 3, "tanh": 2, "pow": 3, "sqrt": 0, "rsqrt": 0, "div": 0}
+
+
+def dev_array(host, shape=None, dtype=None):
+    """Upload a (comps, n) numpy array into an Array with capacity padding."""
+    host = np.asarray(host)
+    if host.ndim == 1:
+        host = host[None, :]
+    dt = dtype or ("f64" if host.dtype == np.float64 else "f32")
+    arr = ag.Array(dt, shape or (host.shape[0],), host.shape[1])
+    arr.upload(host)
+    return arr
+
+
+def uniform_host(oracle, seed, sub, lo, hi, comps, n, f32=False):
+    key = oracle.substream_key(oracle.generator_key(seed), sub)
+    if f32:
+        return oracle.fill_uniform_f32(key, lo, hi, comps, n)
+    return oracle.fill_uniform_f64(key, lo, hi, comps, n)
+
+
+# ---------------------------------------------------------------------------
+# Philox streams
+# ---------------------------------------------------------------------------
+def test_philox_golden_rows_on_device(philox_golden):
+    """Golden rows with counter < 16: uniform(0,1) of the leaf is the raw
+    uniform01 draw when key ^ salt = seed (lo + (hi-lo)*u = u exactly)."""
+    SALT_U = 0x243F6A8885A308D3
+    SALT_N = 0x13198A2E03707344
+    rows = [r for r in philox_golden["core"] if r["counter"] < 16]
+    assert len(rows) >= 150
+    groups = {}
+    for r in rows:
+        groups.setdefault((r["seed"], r["global"]), []).append(r)
+    for (seed, glob), rs in groups.items():
+        for f32 in (False, True):
+            dt = "f32" if f32 else "f64"
+            out = ag.Array(dt, (16,), 1)
+            leaf = ag.expr.RandomLeaf("uniform", seed ^ SALT_U, 16, (0.0, 1.0))
+            ag.assign(out, leaf, sample_offset=glob, contract=0)
+            nor = ag.Array(dt, (16,), 1)
+            nleaf = ag.expr.RandomLeaf("normal", seed ^ SALT_N, 16, (0.0, 1.0))
+            ag.assign(nor, nleaf, sample_offset=glob, contract=0)
+            u = out.host()[:, 0]
+            z = nor.host()[:, 0]
+            for r in rs:
+                c = r["counter"]
+                if f32:
+                    assert np.float32(u[c]).view(np.uint32) == r["uniform_float_bits"]
+                    assert abs(z[c] - r["normal_float"]) <= 1e-5 * (1 + abs(r["normal_float"]))
+                else:
+                    assert np.float64(u[c]).view(np.uint64) == r["uniform_double_bits"]
+                    assert abs(z[c] - r["normal_double"]) <= 1e-12 * (1 + abs(r["normal_double"]))
+
+
+@pytest.mark.parametrize("n", [1, 31, 37, 1000, 4097, 1 << 20])
+def test_uniform_fill_bit_exact(oracle, n):
+    a = ag.Array("f64", (3,), n)
+    ag.assign(a, ag.Generator(42).substream(0).uniform(3, -1.0, 1.0))
+    ref = uniform_host(oracle, 42, 0, -1.0, 1.0, 3, n)
+    assert np.array_equal(a.host(), ref)
+    f = ag.Array("f32", (3,), n)
+    ag.assign(f, ag.Generator(3).substream(0).uniform(3, -1.0, 1.0))
+    assert np.array_equal(f.host(), uniform_host(oracle, 3, 0, -1.0, 1.0, 3, n, f32=True))
+
+
+def test_uniform_fill_matches_reference_fixture(ref_cases):
+    a = ag.Array("f64", (3,), 1000)
+    ag.assign(a, ag.Generator(7).substream(2).uniform(3, -4.0, 4.0))
+    assert np.array_equal(a.host(), ref_cases["cfg2a_c"])
+
+
+def test_normal_fill_config2b(oracle, ref_cases):
+    x = ag.Array("f64", (1,), 4096)
+    ag.assign(x, ag.Generator(7).substream(4).normal(1, 0.0, 1.0))
+    got = x.host()
+    ref = ref_cases["cfg2b_x"]
+    assert np.all(np.abs(got - ref) <= 1e-12 * (1 + np.abs(ref)))
+    # and at 2^20 against the oracle
+    n = 1 << 20
+    y = ag.Array("f64", (1,), n)
+    ag.assign(y, ag.Generator(7).substream(4).normal(1, 0.0, 1.0))
+    key = ag.Generator(7).substream(4).key
+    r = oracle.fill_normal_f64(key, 0.0, 1.0, 1, n)
+    assert np.all(np.abs(y.host() - r) <= 1e-12 * (1 + np.abs(r)))
+
+
+def test_normal_fill_sample_offset(oracle):
+    n = 5000
+    y = ag.Array("f64", (1,), n)
+    ag.assign(y, ag.Generator(9).normal(1, 2.0, 0.5), sample_offset=123456)
+    r = oracle.fill_normal_f64(ag.Generator(9).key, 2.0, 0.5, 1, n, sample_offset=123456)
+    assert np.all(np.abs(y.host() - r) <= 1e-12 * (1 + np.abs(r)))
+
+
+# ---------------------------------------------------------------------------
+# The benchmark expressions
+# ---------------------------------------------------------------------------
+def _cfg1(a, b, c):
+    return a + b * c + ag.cwiseSin(a) * ag.cwiseExp((c * c) * (-1.0))
+
+
+def _cfg2a(a, b, c, d0):
+    return ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c)) + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0)
+
+
+@pytest.mark.parametrize("contract", [0, 1])
+def test_config1_parity(oracle, ref_cases, contract):
+    z = ref_cases
+    a, b, c = (dev_array(z[k]) for k in ("cfg1_a", "cfg1_b", "cfg1_c"))
+    d = ag.Array("f64", (3,), 1000)
+    ag.assign(d, _cfg1(a.view(), b.view(), c.view()), contract=contract)
+    A, B, C = z["cfg1_a"], z["cfg1_b"], z["cfg1_c"]
+    scale = np.maximum.reduce([np.abs(A), np.abs(B * C), np.abs(np.sin(A) * np.exp(-C * C))])
+    assert_ulp(d.host(), z["cfg1_d"], 4, scale, "config 1 vs reference")
+
+
+def test_config1_full_size(oracle):
+    n = 1 << 20
+    A, B, C = (uniform_host(oracle, 42, k, -1.0, 1.0, 3, n) for k in range(3))
+    arrs = [ag.Array("f64", (3,), n) for _ in range(3)]
+    for k, arr in enumerate(arrs):
+        ag.assign(arr, ag.Generator(42).substream(k).uniform(3, -1.0, 1.0))
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, _cfg1(*(x.view() for x in arrs)))
+    ref = oracle.cfg1(A, B, C)
+    scale = np.maximum.reduce([np.abs(A), np.abs(B * C), np.abs(np.sin(A) * np.exp(-C * C))])
+    assert_ulp(d.host(), ref, 4, scale, "config 1, 2^20 samples")
+
+
+@pytest.mark.parametrize("math", [0, 1])
+def test_config2a_parity(oracle, ref_cases, math):
+    z = ref_cases
+    ins = [dev_array(z[k]) for k in ("cfg2a_a", "cfg2a_b", "cfg2a_c", "cfg2a_d0")]
+    d = ag.Array("f64", (3,), 1000)
+    ag.assign(d, _cfg2a(*(x.view() for x in ins)), math=math)
+    A, B, C, D0 = (z[k] for k in ("cfg2a_a", "cfg2a_b", "cfg2a_c", "cfg2a_d0"))
+    scale = np.maximum(np.abs(np.sqrt(A * A + B * B) * np.log1p(np.abs(C))), np.abs(1 / np.sqrt(1 + D0 * D0)))
+    assert_ulp(d.host(), z["cfg2a_d"], 4, scale, "config 2a vs reference")
+
+
+def test_config2a_subsample_at_2p24(oracle):
+    """Large n: evaluate on device at 2^24 samples and check 2^15 random
+    samples against the oracle evaluated on the same inputs."""
+    n = 1 << 24
+    arrs = [ag.Array("f64", (3,), n) for _ in range(4)]
+    for k, arr in enumerate(arrs):
+        ag.assign(arr, ag.Generator(7).substream(k).uniform(3, -4.0, 4.0))
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, _cfg2a(*(x.view() for x in arrs)))
+    idx = torch.randint(0, n, (1 << 15,), generator=torch.Generator().manual_seed(1)).cuda()
+    sub = [np.ascontiguousarray(x.data[:, idx].cpu().numpy()) for x in arrs]
+    ref = oracle.cfg2a(*sub)
+    got = d.data[:, idx].cpu().numpy()
+    A, B, C, D0 = sub
+    scale = np.maximum(np.abs(np.sqrt(A * A + B * B) * np.log1p(np.abs(C))), np.abs(1 / np.sqrt(1 + D0 * D0)))
+    assert_ulp(got, ref, 4, scale, "config 2a, 2^24 samples")
+
+
+# ---------------------------------------------------------------------------
+# Node corpus against the reference fixtures
+# ---------------------------------------------------------------------------
+CW = {
+    "cw_sqrt": (lambda x, y: ag.cwiseSqrt(x), 0), "cw_rsqrt": (lambda x, y: ag.cwiseRsqrt(x), 0),
+    "cw_exp": (lambda x, y: ag.cwiseExp(x), 2), "cw_log": (lambda x, y: ag.cwiseLog(x), 2),
+    "cw_sin": (lambda x, y: ag.cwiseSin(x), 3), "cw_cos": (lambda x, y: ag.cwiseCos(x), 3),
+    "cw_tan": (lambda x, y: ag.cwiseTan(x), 3), "cw_asin": (lambda x, y: ag.cwiseAsin(x), 3),
+    "cw_acos": (lambda x, y: ag.cwiseAcos(x), 3), "cw_atan": (lambda x, y: ag.cwiseAtan(x), 3),
+    "cw_tanh": (lambda x, y: ag.cwiseTanh(x), 2), "cw_abs": (lambda x, y: ag.cwiseAbs(x), 0),
+    "cw_sign": (lambda x, y: ag.cwiseSign(x), 0), "cw_mins": (lambda x, y: ag.cwiseMin(x, 0.25), 0),
+    "cw_maxs": (lambda x, y: ag.cwiseMax(x, -0.25), 0), "cw_min": (lambda x, y: ag.cwiseMin(x, y), 0),
+    "cw_max": (lambda x, y: ag.cwiseMax(x, y), 0), "cw_clamp": (lambda x, y: ag.clamp(x, -0.5, 0.5), 0),
+    "cw_div": (lambda x, y: ag.cwiseDiv(x, y), 0), "cw_pow": (lambda x, y: ag.cwisePow(ag.cwiseAbs(x), y), 3),
+    "cw_pows": (lambda x, y: ag.cwisePow(ag.cwiseAbs(x), 1.75), 3), "cw_scale": (lambda x, y: 2.5 * x, 0),
+    "cw_divs": (lambda x, y: x / 3.0, 0), "cw_sub": (lambda x, y: x - y, 0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CW))
+def test_elementwise_nodes(ref_cases, name):
+    fn, ulps = CW[name]
+    x, y = dev_array(ref_cases["cw_x"]), dev_array(ref_cases["cw_y"])
+    d = ag.Array("f64", (1,), x.n)
+    ag.assign(d, fn(x.view(), y.view()), contract=0)
+    got, ref = d.host(), ref_cases[name]
+    if ulps == 0:
+        assert np.array_equal(got, ref, equal_nan=True), name
+    else:
+        assert ulp_diff(got, ref).max() <= ulps, (name, ulp_diff(got, ref).max())
+
+
+GEO = {
+    "geo_cross": (lambda z: z["geo_a"].cross(z["geo_b"]), (3,)),
+    "geo_qrot": (lambda z: z["geo_q"].quatRotate(z["geo_a"]), (3,)),
+    "geo_qmul": (lambda z: z["geo_q"].quatMul(z["geo_p"]), (4,)),
+    "geo_unit_item": (lambda z: z["geo_a"].unitVector(), (3,)),
+    "geo_unit": (lambda z: z["geo_a"] * z["geo_a"].rNorm().at_sample0(), (3,)),
+    "geo_inv": (lambda z: z["geo_m"].inverse(), (3, 3)),
+    "geo_det": (lambda z: z["geo_m"].det(), ()),
+    "geo_trace": (lambda z: z["geo_m"].trace(), ()),
+}
+
+
+@pytest.mark.parametrize("name", sorted(GEO))
+def test_geometry_nodes_bit_exact(ref_cases, name):
+    fn, shape = GEO[name]
+    shapes = {"geo_a": (3,), "geo_b": (3,), "geo_q": (4,), "geo_p": (4,), "geo_m": (3, 3)}
+    views = {k: dev_array(ref_cases[k], shape=s).view() for k, s in shapes.items()}
+    n = ref_cases["geo_a"].shape[1]
+    d = ag.Array("f64", shape if shape else (1,), n)
+    ag.assign(d, fn(views), contract=0)
+    assert np.array_equal(d.host(), ref_cases[name].reshape(d.host().shape)), name
+
+
+def test_dot_fold_bit_exact(ref_cases):
+    z = ref_cases
+    x, y = dev_array(z["dot_x"]), dev_array(z["dot_y"])
+    d = ag.Array("f64", (1,), 600)
+    ag.assign(d, x.view().dot(y.view()), contract=0)
+    assert np.array_equal(d.host(), z["dot_d"])
+    xf, yf = dev_array(z["dot_xf"]), dev_array(z["dot_yf"])
+    f = ag.Array("f32", (1,), 600)
+    ag.assign(f, xf.view().dot(yf.view()), contract=0)
+    assert np.array_equal(f.host(), z["dot_f"])
+
+
+@pytest.mark.parametrize("name", ["leaf_lognormal", "leaf_exponential", "leaf_bernoulli"])
+def test_distribution_leaves(ref_cases, name):
+    g = ag.Generator(11)
+    leaf = {"leaf_lognormal": g.lognormal(2, 0.1, 0.5), "leaf_exponential": g.exponential(2, 1.5),
+            "leaf_bernoulli": g.bernoulli(2, 0.3)}[name]
+    d = ag.Array("f64", (2,), 1000)
+    ag.assign(d, leaf, contract=0)
+    ref = ref_cases[name]
+    if name == "leaf_bernoulli":
+        assert np.array_equal(d.host(), ref)
+    else:
+        assert np.all(np.abs(d.host() - ref) <= 1e-12 * (1 + np.abs(ref))), name
+
+
+def test_uniform_item_parameters(ref_cases):
+    g = ag.Generator(11)
+    leaf = g.uniform(2, ag.stack(ag.expr.Scalar(-2.0), ag.expr.Scalar(10.0)),
+                     ag.stack(ag.expr.Scalar(2.0), ag.expr.Scalar(11.0)))
+    d = ag.Array("f64", (2,), 1000)
+    ag.assign(d, leaf, contract=0)
+    assert np.array_equal(d.host(), ref_cases["leaf_uniform_item"])
+
+
+# ---------------------------------------------------------------------------
+# Interpreter-checked cases (arbitrary trees against the oracle)
+# ---------------------------------------------------------------------------
+def _oracle_eval(oracle, expr, dst_dtype, dst_shape, n, op="set", mode=0, out=None):
+    ctx = ag.IrContext()
+    ir = ag.expr.plan_text(dst_dtype, dst_shape, op, expr, ctx)
+    ops = []
+    for (ptr, pitch, dt, comps, owner) in ctx.operands:
+        ops.append(np.ascontiguousarray(owner.data.cpu().numpy()))
+    comps = 1
+    for s in dst_shape:
+        comps *= s
+    npdt = np.float64 if (dst_dtype == "f64" or mode) else np.float32
+    res, red = oracle.eval_ir(ir, n, ops, scalars=ctx.scalars, keys=ctx.keys, dst_comps=comps, dst_dtype=npdt,
+                              mode=mode, out=out, reduce=op in ("sum", "setsum"))
+    return res, red
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 37, 255, 256, 257, 511, 513, 1025, 4099])
+def test_ragged_sizes_and_tails(oracle, n):
+    a = ag.Array("f64", (3,), n)
+    b = ag.Array("f64", (3,), n)
+    ag.assign(a, ag.Generator(1).uniform(3, -2.0, 2.0))
+    ag.assign(b, ag.Generator(2).uniform(3, -2.0, 2.0))
+    e = a.view().cross(b.view()) + a.view() * 0.5
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, e, contract=0)
+    ref, _ = _oracle_eval(oracle, e, "f64", (3,), n)
+    assert np.array_equal(d.host(), ref[:, :n])
+
+
+def test_misaligned_operands_take_the_scalar_kernel(oracle):
+    n = 1001
+    base = torch.zeros((3, 1100), dtype=torch.float64, device="cuda")
+    sub = base[:, 1:]   # plane start 8 bytes past a 16-byte boundary
+    a = ag.Array.wrap(sub.contiguous(), n=n)
+    ag.assign(a, ag.Generator(5).uniform(3, -1.0, 1.0))
+    mis = ag.expr.Operand(base.data_ptr() + 8, 1100, "f64", (3,))
+    base[:, 1:1 + n] = a.data[:, :n]
+    d1 = ag.Array("f64", (3,), n)
+    d2 = ag.Array("f64", (3,), n)
+    ag.assign(d1, a.view() * a.view() + 1.0, contract=0)
+    ag.assign(d2, mis * mis + 1.0, contract=0)
+    assert np.array_equal(d1.host(), d2.host())
+
+
+def test_assign_add_and_sub(oracle):
+    n = 3000
+    a = ag.Array("f64", (3,), n)
+    ag.assign(a, ag.Generator(3).uniform(3, -1.0, 1.0))
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, ag.constant(1.0, (3,)))
+    ag.assign_add(d, a.view() * 2.0, contract=0)
+    ag.assign_sub(d, a.view(), contract=0)
+    A = a.host()
+    assert np.array_equal(d.host(), (1.0 + A * 2.0) - A)
+
+
+def test_guarded_inverse_and_matmul(oracle):
+    n = 4096
+    m = ag.Array("f64", (3, 3), n)
+    ag.assign(m, ag.Generator(8).uniform(9, -1.0, 1.0).reshape((3, 3)))
+    M = m.view()
+    e = ag.select(ag.cwiseAbs(M.det()) > 1e-300, M.inverse(), ag.constant(0.0, (3, 3)))
+    d = ag.Array("f64", (3, 3), n)
+    ag.assign(d, e, contract=0)
+    ref, _ = _oracle_eval(oracle, e, "f64", (3, 3), n)
+    assert np.array_equal(d.host(), ref[:, :n])
+    e2 = M.matmul(M.transpose())
+    d2 = ag.Array("f64", (3, 3), n)
+    ag.assign(d2, e2, contract=0)
+    ref2, _ = _oracle_eval(oracle, e2, "f64", (3, 3), n)
+    assert np.array_equal(d2.host(), ref2[:, :n])
+
+
+def test_float_plan_transcendentals(oracle):
+    n = 1 << 16
+    x = ag.Array("f32", (3,), n)
+    ag.assign(x, ag.Generator(4).uniform(3, -3.0, 3.0))
+    e = ag.cwiseSin(x.view()) * ag.cwiseExp(x.view() * 0.5) + ag.cwiseTanh(x.view())
+    d = ag.Array("f32", (3,), n)
+    ag.assign(d, e)
+    ref, _ = _oracle_eval(oracle, e, "f32", (3,), n)
+    X = x.host().astype(np.float64)
+    scale = np.maximum(np.abs(np.sin(X) * np.exp(0.5 * X)), np.abs(np.tanh(X))).astype(np.float32)
+    assert_ulp(d.host(), ref[:, :n], 8, scale, "float plan")
+
+
+# ---------------------------------------------------------------------------
+# Global compensated sums
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 37, 512, 513, 100000, 1 << 20])
+def test_global_sum_f64(oracle, n):
+    x = ag.Array("f64", (8,), n)
+    y = ag.Array("f64", (8,), n)
+    ag.assign(x, ag.Generator(21).uniform(8, -1.0, 1.0))
+    ag.assign(y, ag.Generator(22).uniform(8, -1.0, 1.0))
+    e = x.view().dot(y.view())
+    r1 = ag.global_sum(e, n).cpu().numpy()
+    r2 = ag.global_sum(e, n).cpu().numpy()
+    assert np.array_equal(r1, r2), "sum must be deterministic"
+    _, ref = _oracle_eval(oracle, e, "f64", (), n, op="sum", mode=2)
+    tot = r1[0] + r1[1]
+    absmag = np.abs(x.host() * y.host()).sum()
+    assert abs(tot - (ref[0] + ref[1])) <= 4e-16 * absmag + 1e-300
+
+
+def test_setsum_writes_and_sums(oracle):
+    n = 50000
+    x = ag.Array("f32", (8,), n)
+    y = ag.Array("f32", (8,), n)
+    ag.assign(x, ag.Generator(31).uniform(8, -1.0, 1.0))
+    ag.assign(y, ag.Generator(32).uniform(8, -1.0, 1.0))
+    d = ag.Array("f32", (1,), n)
+    red = torch.zeros(2, dtype=torch.float64, device="cuda")
+    ag.assign(d, x.view().dot(y.view()), op="setsum", reduce_out=red, contract=0)
+    ref, _ = _oracle_eval(oracle, x.view().dot(y.view()), "f32", (), n)
+    assert np.array_equal(d.host()[0], ref[0, :n])
+    s = red.cpu().numpy()
+    exact = np.sum(ref[0, :n].astype(np.float64))
+    assert abs((s[0] + s[1]) - exact) <= 1e-13 * np.abs(ref[0, :n]).sum()
+
+
+# ---------------------------------------------------------------------------
+# Errors at the boundary
+# ---------------------------------------------------------------------------
+def test_launch_errors_are_reported():
+    a = ag.Array("f64", (3,), 100)
+    plan = ag.get_plan("(plan f64 [3] set (add (in 0 f64 [3]) (in 1 f64 [3])))")
+    args = ag._abi.AetherLaunch()
+    args.n = 100
+    args.dst = a.data.data_ptr()
+    args.dst_pitch = a.capacity
+    args.n_operands = 0
+    rc = ag._abi.lib().aether_plan_launch(plan.handle, ctypes.byref(args), None)
+    assert rc == 1 and b"operands" in ag._abi.lib().aether_last_error()
+    with pytest.raises(ag.AetherError, match="reduce_out"):
+        ag.prepare(a, a.view(), op="setsum")(None)
