@@ -23,7 +23,8 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp"]
 DEVICE_SOURCES = []
-EMBED = [("kAgDeviceSrc", "device/ag_device.cuh"), ("kAgEmu64Src", "device/ag_emu64.cuh")]
+EMBED = [("kAgDeviceSrc", "device/ag_device.cuh"), ("kAgEmu64Src", "device/ag_emu64.cuh"),
+         ("kAgEmu64TablesSrc", "device/ag_emu64_tables.cuh")]
 EXPORT_PREFIX = "aether_"
 
 

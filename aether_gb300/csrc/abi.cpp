@@ -123,6 +123,7 @@ static_assert(sizeof(AgArgsHost) == 504, "AgArgs layout");
 struct PlanObj {
     ag::Plan plan;
     ag::Lowering low;
+    std::string name;
     std::string source;
     ag::Compiled compiled;
     cudaLibrary_t library = nullptr;
@@ -325,14 +326,15 @@ AG_EXPORT int aether_plan_create(const char* ir, const AetherLowering* lowering,
         if (P->vec != 1 && P->vec != 2 && P->vec != 4) throw std::runtime_error("plan_create: vec must be 1, 2 or 4");
         if (P->low.math == 1 && P->plan.dst_dtype != ag::DType::F64)
             throw std::runtime_error("plan_create: emulated FP64 applies to f64 plans");
-        P->source = ag::generate_source(P->plan, P->low);
+        P->name = ag::kernel_base(P->plan, ir);
+        P->source = ag::generate_source(P->plan, P->low, P->name);
         ck(cudaFree(nullptr), "CUDA context");   // make the primary context current
         cudaGetDevice(&P->dev);
         P->compiled = ag::compile_cached(P->source, "plan");
         ck(cudaLibraryLoadData(&P->library, P->compiled.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
            "cudaLibraryLoadData");
-        ck(cudaLibraryGetKernel(&P->fv, P->library, "ag_plan_v"), "cudaLibraryGetKernel(ag_plan_v)");
-        ck(cudaLibraryGetKernel(&P->fs, P->library, "ag_plan_s"), "cudaLibraryGetKernel(ag_plan_s)");
+        ck(cudaLibraryGetKernel(&P->fv, P->library, (P->name + "_v").c_str()), "cudaLibraryGetKernel");
+        ck(cudaLibraryGetKernel(&P->fs, P->library, (P->name + "_s").c_str()), "cudaLibraryGetKernel");
         cudaFuncAttributes fa{};
         ck(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(P->fv)), "cudaFuncGetAttributes");
         P->registers = fa.numRegs;
@@ -480,7 +482,7 @@ AG_EXPORT int aether_plan_generate(const char* ir, const AetherLowering* lowerin
             if (lowering->math >= 0) low.math = lowering->math;
             if (lowering->min_blocks > 0) low.min_blocks = lowering->min_blocks;
         }
-        const std::string src = ag::generate_source(plan, low);
+        const std::string src = ag::generate_source(plan, low, ag::kernel_base(plan, ir));
         if (len) *len = src.size();
         if (buf && cap) {
             const size_t n = std::min(cap - 1, src.size());

@@ -1,47 +1,430 @@
-// ag_emu64.cuh -- FP64 math evaluated on the FP32 and integer pipes.
+// ag_emu64.cuh -- FP64 expression math on the FP32 and integer pipes.
 //
 // Included by generated kernels lowered with math = 1. On GB300 the FP64 pipe
 // issues about 1.6 operations per clock per SM against about 110 FFMA and 59
-// IMAD, so an FP64 expression kernel with transcendental nodes is bound by the
-// FP64 pipe long before HBM. The functions here keep FP64 inputs and outputs
-// but do the bulk of the arithmetic in float/integer form.
+// IMAD (double <-> float conversions run on the FP64 pipe as well), so an
+// FP64 expression kernel with transcendental nodes is bound by that pipe long
+// before HBM. Here every double is split into a double-float pair
+// (hi + lo, two floats, about 48 significant bits) with integer operations,
+// the expression is evaluated in double-float arithmetic, and each output is
+// reassembled into a double with one FP64 addition.
+//
+// Accuracy: relative error about 2^-46 per function (a few tens of double
+// ulps in the worst case), against 2^-53 for the native pipe. Samples whose
+// inputs leave [2^-60, 2^60] in magnitude, whose trig arguments exceed
+// 4096*pi/2, or whose outputs are not finite normal values above 2^-90 are
+// recomputed by the generated code with native FP64 (the fallback path), so
+// range, special values and large-argument reduction keep FP64 semantics.
+//
+// Methods (all from the published literature, constants computed by
+// gen_emu64_tables.py): Knuth two-sum, Dekker fast-two-sum, FMA two-product;
+// double-word addition/multiplication of Joldes, Muller & Popescu (2017);
+// Newton-Raphson square root and reciprocal square root from a hardware seed;
+// table-driven exp (Tang 1989) and log (Tang 1990); Cody-Waite reduction by
+// pi/2 with a 1/32-spaced sine/cosine table; Box-Muller from exact integer
+// uniforms.
 #pragma once
+
+#include "ag_emu64_tables.cuh"
 
 namespace ag {
 namespace e64 {
 
-// Until a node has an emulated form it falls back to the native one.
-using ag::f_abs;
-using ag::f_acos;
-using ag::f_asin;
-using ag::f_atan;
-using ag::f_atan2;
-using ag::f_cbrt;
-using ag::f_ceil;
-using ag::f_cos;
-using ag::f_cosh;
-using ag::f_erf;
-using ag::f_exp;
-using ag::f_exp2;
-using ag::f_expm1;
-using ag::f_floor;
-using ag::f_hypot;
-using ag::f_log;
-using ag::f_log10;
-using ag::f_log1p;
-using ag::f_log2;
-using ag::f_max;
-using ag::f_min;
-using ag::f_neg;
-using ag::f_pow;
-using ag::f_rsqrt;
-using ag::f_sign;
-using ag::f_sin;
-using ag::f_sinh;
-using ag::f_sqrt;
-using ag::f_tan;
-using ag::f_tanh;
-using ag::f_trunc;
+struct df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df mk(float h, float l) {
+    df r;
+    r.hi = h;
+    r.lo = l;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Error-free transformations.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return mk(s, e);
+}
+// Requires |a| >= |b| or a == 0.
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float e = __fsub_rn(b, __fsub_rn(s, a));
+    return mk(s, e);
+}
+__device__ __forceinline__ df two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    return mk(p, e);
+}
+
+// ---------------------------------------------------------------------------
+// Double-float arithmetic.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df neg(df x) { return mk(-x.hi, -x.lo); }
+
+// Accurate sum, relative error <= 3u^2 even under cancellation.
+__device__ __forceinline__ df add(df x, df y) {
+    const df s = two_sum(x.hi, y.hi);
+    const df t = two_sum(x.lo, y.lo);
+    const float c = __fadd_rn(s.lo, t.hi);
+    const df v = fast_two_sum(s.hi, c);
+    const float w = __fadd_rn(t.lo, v.lo);
+    return fast_two_sum(v.hi, w);
+}
+__device__ __forceinline__ df sub(df x, df y) { return add(x, neg(y)); }
+// Sum of terms that cannot cancel (same sign, or |y| well below |x|).
+__device__ __forceinline__ df add_fast(df x, df y) {
+    const df s = two_sum(x.hi, y.hi);
+    const float v = __fadd_rn(__fadd_rn(x.lo, y.lo), s.lo);
+    return fast_two_sum(s.hi, v);
+}
+__device__ __forceinline__ df add(df x, float y) {
+    const df s = two_sum(x.hi, y);
+    const float v = __fadd_rn(x.lo, s.lo);
+    return fast_two_sum(s.hi, v);
+}
+__device__ __forceinline__ df mul(df x, df y) {
+    const df c = two_prod(x.hi, y.hi);
+    const float tl0 = __fmul_rn(x.lo, y.lo);
+    const float tl1 = __fmaf_rn(x.hi, y.lo, tl0);
+    const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
+    return fast_two_sum(c.hi, __fadd_rn(c.lo, cl2));
+}
+__device__ __forceinline__ df mul(df x, float y) {
+    const df c = two_prod(x.hi, y);
+    return fast_two_sum(c.hi, __fmaf_rn(x.lo, y, c.lo));
+}
+__device__ __forceinline__ df sqr(df x) {
+    const df c = two_prod(x.hi, x.hi);
+    return fast_two_sum(c.hi, __fmaf_rn(2.0f * x.hi, x.lo, c.lo));
+}
+// Scale by an exact power of two.
+__device__ __forceinline__ df scale(df x, float p2) { return mk(__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)); }
+
+// Hardware seeds (MUFU). The host branch exists only so the double-float
+// algorithms can be checked by a host build of this header.
+__device__ __forceinline__ float rcp_approx(float x) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
+
+// Reciprocal: FP32 seed refined by two double-float Newton steps.
+__device__ __forceinline__ df recip(df y) {
+    float r = rcp_approx(y.hi);
+    r = __fmaf_rn(r, __fmaf_rn(-y.hi, r, 1.0f), r);
+    // e = 1 - y*r, computed exactly enough in double-float
+    const df yr = mul(y, r);
+    const float e = __fsub_rn(__fsub_rn(1.0f, yr.hi), yr.lo);
+    return fast_two_sum(r, __fmul_rn(r, e));
+}
+__device__ __forceinline__ df div(df x, df y) {
+    const float q1 = __fmul_rn(x.hi, rcp_approx(y.hi));
+    const df r = sub(x, mul(y, q1));
+    const float q2 = __fmul_rn(r.hi, rcp_approx(y.hi));
+    const df q = fast_two_sum(q1, q2);
+    const df r2 = sub(x, mul(y, q));
+    return add(q, __fmul_rn(r2.hi, rcp_approx(y.hi)));
+}
+
+__device__ __forceinline__ bool gt(df a, df b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+__device__ __forceinline__ bool lt(df a, df b) { return gt(b, a); }
+__device__ __forceinline__ bool ge(df a, df b) { return !lt(a, b); }
+__device__ __forceinline__ bool le(df a, df b) { return !gt(a, b); }
+__device__ __forceinline__ bool eq(df a, df b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool ne(df a, df b) { return !eq(a, b); }
+
+// ---------------------------------------------------------------------------
+// double <-> double-float, with integer operations only (no F2F).
+// ---------------------------------------------------------------------------
+// |x| in [2^-60, 2^60]: the range where products of a few operands stay
+// normal floats.
+__device__ __forceinline__ bool in_range(double x) {
+    const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+    return ex - (1023u - 60u) <= 120u;
+}
+__device__ __forceinline__ df from_double(double x) {
+    const unsigned h32 = (unsigned)__double2hiint(x);
+    const unsigned l32 = (unsigned)__double2loint(x);
+    const unsigned sign = h32 & 0x80000000u;
+    const int ex = (int)((h32 >> 20) & 0x7ffu);
+    // hi: the top 24 significant bits (truncated), re-biased to float
+    const unsigned hb = ((((h32 & 0x7fffffffu) - (896u << 20)) << 3) | (l32 >> 29)) | sign;
+    // lo: the remaining 29 bits, rounded to a float and scaled by 2^(ex-1075)
+    const float lo = __fmul_rn(__uint2float_rn(l32 & 0x1fffffffu), __int_as_float((ex - 948) << 23));
+    return fast_two_sum(__int_as_float(hb), __int_as_float(__float_as_int(lo) ^ sign));
+}
+// A normal float (or zero) as a double.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned b = (unsigned)__float_as_int(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const double d = __hiloint2double((int)hi, (int)(b << 29));
+    return e == 0u ? 0.0 : d;
+}
+__device__ __forceinline__ double to_double(df v) { return __dadd_rn(f2d(v.hi), f2d(v.lo)); }
+// A result that reassembles exactly: finite, normal and away from underflow.
+__device__ __forceinline__ bool out_ok(df v) {
+    const unsigned e = ((unsigned)__float_as_int(v.hi) >> 23) & 0xffu;
+    return e - 37u <= 216u;   // |hi| in [2^-90, 2^127)
+}
+// 0 < w < 2^54 as a double-float: the top 24 significant bits exactly, the
+// rest rounded once (2^-48 relative).
+__device__ __forceinline__ df from_u64(ag_u64 w) {
+    const int sh = 40 - __clzll((long long)w);   // bits below the leading 24
+    if (sh <= 0) return mk(__uint2float_rn((ag_u32)w), 0.0f);
+    const float h = __fmul_rn(__uint2float_rn((ag_u32)(w >> sh)), __int_as_float((sh + 127) << 23));
+    const float l = __uint2float_rn((ag_u32)(w & ((1ull << sh) - 1ull)));
+    return fast_two_sum(h, l);
+}
+__device__ __forceinline__ float p2f(int k) { return __int_as_float((k + 127) << 23); }   // 2^k, |k| <= 126
+// Round to nearest integer for |x| < 2^22 with one FP32 add (no conversion unit).
+__device__ __forceinline__ float rint_f(float x) { return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f); }
+__device__ __forceinline__ int rint_i(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000; }
+
+// ---------------------------------------------------------------------------
+// Square root and reciprocal square root (Newton-Raphson, one double-float
+// correction of a refined hardware seed).
+// ---------------------------------------------------------------------------
+// Hardware rsqrt seed refined once in FMA form to about 2^-24.5:
+// y += (y/2) (1 - x y^2), the residual taken from an FMA.
+__device__ __forceinline__ float rsqrt_seed(float x) {
+    const float y = rsqrt_approx(x);
+    const float e = __fmaf_rn(-__fmul_rn(x, y), y, 1.0f);
+    return __fmaf_rn(__fmul_rn(0.5f, y), e, y);
+}
+__device__ __forceinline__ df sqrt_(df x) {
+    const float y = rsqrt_seed(x.hi);
+    const float s = __fmul_rn(x.hi, y);
+    const df p = two_prod(s, s);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p.hi), p.lo), x.lo);
+    const df res = fast_two_sum(s, __fmul_rn(r, 0.5f * y));
+    return x.hi > 0.0f ? res : (x.hi == 0.0f ? mk(0.0f, 0.0f) : mk(__int_as_float(0x7fc00000), 0.0f));
+}
+__device__ __forceinline__ df rsqrt_(df x) {
+    const float y = rsqrt_seed(x.hi);
+    const df xyy = mul(mul(x, y), y);
+    const float e = __fsub_rn(__fsub_rn(1.0f, xyy.hi), xyy.lo);
+    const df res = fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
+    return x.hi > 0.0f ? res : mk(__int_as_float(0x7fc00000), 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// exp: x = (64k + j) ln2/64 + r, |r| <= ln2/128; e^x = 2^k 2^(j/64) e^r.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df exp_(df x) {
+    const float mf = rint_f(__fmul_rn(x.hi, AG_INV_LN2_64));
+    const int m = rint_i(__fmul_rn(x.hi, AG_INV_LN2_64));
+    const float r1 = __fmaf_rn(-mf, AG_LN2_64_1, x.hi);   // exact (Sterbenz)
+    df r = two_sum(r1, x.lo);
+    r = sub(r, two_prod(mf, AG_LN2_64_2));
+    r = add(r, __fmul_rn(-mf, AG_LN2_64_3));
+    // e^r - 1 = r + r^2/2 + r^3 (1/6 + r/24 + r^2/120)
+    const float rh = r.hi;
+    const float tail = __fmul_rn(__fmul_rn(rh, __fmul_rn(rh, rh)),
+                                 __fmaf_rn(rh, __fmaf_rn(rh, 8.33333333e-3f, 4.16666667e-2f), 1.66666667e-1f));
+    df p = add_fast(r, scale(sqr(r), 0.5f));
+    p = add(p, tail);
+    const int j = m & 63;
+    int k = m >> 6;
+    const df T = mk(__ldg(&kExp2TabHi[j]), __ldg(&kExp2TabLo[j]));
+    const df res = add_fast(T, mul(T, p));
+    k = k < -126 ? -126 : (k > 126 ? 126 : k);
+    return scale(res, p2f(k));
+}
+
+// ---------------------------------------------------------------------------
+// log: y = 2^e m, m in [0.75, 1.5), i = round(128 (m - 1)), c_i ~ 1/(1 + i/128)
+// (c_0 = 1), t = y 2^-e c_i - 1 (|t| < 2^-7), log y = e ln2 - log c_i + log(1+t).
+// log_s(s, x) is log(s + x) for s in {0, 1}: log for s = 0, log1p for s = 1,
+// with t formed from s and x separately so 1 + x is never rounded.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df log1p_poly(df t) {
+    const df t2 = sqr(t);
+    const df t3 = mul(t2, t);
+    const float th = t.hi;
+    const float t4 = __fmul_rn(__fmul_rn(th, th), __fmul_rn(th, th));
+    const float tail = __fmul_rn(t4, __fmaf_rn(th, __fmaf_rn(th, __fmaf_rn(th, 0.142857143f, -0.166666667f), 0.2f), -0.25f));
+    df q = add(mul(t3, mk(AG_THIRD_HI, AG_THIRD_LO)), tail);
+    q = add_fast(scale(t2, -0.5f), q);
+    return add_fast(t, q);
+}
+__device__ __forceinline__ df log_s(float s, df x) {
+    const float yh = __fadd_rn(s, x.hi);
+    const int bits = __float_as_int(yh);
+    int e = ((bits >> 23) & 0xff) - 127;
+    int mb = (bits & 0x007fffff) | 0x3f800000;
+    if (bits & 0x00400000) {   // m >= 1.5: use m/2 and e+1
+        mb -= 0x00800000;
+        e += 1;
+    }
+    const float m = __int_as_float(mb);
+    const int i = rint_i(__fmul_rn(__fsub_rn(m, 1.0f), 128.0f));
+    const float c = __ldg(&kLogC[i + 32]);
+    const float A = __fmul_rn(c, p2f(-e));         // c 2^-e, exact
+    const df B = two_sum(__fmul_rn(s, A), -1.0f);   // s A - 1, exact
+    const df C = mul(x, A);
+    const df t = add(B, C);
+    const df lp = log1p_poly(t);
+    const df L = mk(__ldg(&kLogLHi[i + 32]), __ldg(&kLogLLo[i + 32]));
+    const float fe = (float)e;
+    const df p2 = two_prod(fe, AG_LN2_2);
+    const df E = add(fast_two_sum(__fmul_rn(fe, AG_LN2_1), p2.hi), __fmaf_rn(fe, AG_LN2_3, p2.lo));
+    const df res = add(E, add(L, lp));
+    const bool valid = yh > 0.0f && e > -120 && e < 120;
+    return valid ? res : mk(__int_as_float(0x7fc00000), 0.0f);
+}
+__device__ __forceinline__ df log_(df x) { return log_s(0.0f, x); }
+__device__ __forceinline__ df log1p_(df x) { return log_s(1.0f, x); }
+
+// ---------------------------------------------------------------------------
+// sin/cos: r in [-pi/4, pi/4] split as r = j/32 + t (|t| <= 1/64);
+// sin r = S_j + S_j (cos t - 1) + C_j sin t, cos r = C_j + C_j (cos t - 1) - S_j sin t.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sincos_core(df r, int q, df* so, df* co) {
+    const float jf = rint_f(__fmul_rn(r.hi, 32.0f));
+    const int j = rint_i(__fmul_rn(r.hi, 32.0f));
+    const df t = fast_two_sum(__fsub_rn(r.hi, __fmul_rn(jf, 0.03125f)), r.lo);
+    const df t2 = sqr(t);
+    const float th = t.hi;
+    const float th2 = __fmul_rn(th, th);
+    // sin t = t - t^3/6 + t^5/120
+    const df t3 = mul(t2, t);
+    const df st = add_fast(t, add(mul(t3, mk(-AG_SIXTH_HI, -AG_SIXTH_LO)),
+                                  __fmul_rn(__fmul_rn(t3.hi, th2), 8.33333333e-3f)));
+    // cos t - 1 = -t^2/2 + t^4/24 - t^6/720
+    const float c4 = __fmul_rn(__fmul_rn(th2, th2), __fmaf_rn(th2, -1.38888889e-3f, 4.16666667e-2f));
+    const df cm1 = add(scale(t2, -0.5f), c4);
+    const df S = mk(__ldg(&kSinTabHi[j + 26]), __ldg(&kSinTabLo[j + 26]));
+    const df C = mk(__ldg(&kCosTabHi[j + 26]), __ldg(&kCosTabLo[j + 26]));
+    const df sr = add(add(S, mul(S, cm1)), mul(C, st));
+    const df cr = sub(add(C, mul(C, cm1)), mul(S, st));
+    const int qq = q & 3;
+    const df s0 = (qq & 1) ? cr : sr;
+    const df c0 = (qq & 1) ? sr : cr;
+    *so = (qq & 2) ? neg(s0) : s0;
+    *co = ((qq + 1) & 2) ? neg(c0) : c0;
+}
+// Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.
+__device__ __forceinline__ void sincos_(df x, df* s, df* c, bool& ok) {
+    ok = ok && fabsf(x.hi) < 6000.0f;
+    const float kf = rint_f(__fmul_rn(x.hi, AG_TWO_OVER_PI));
+    const float r1 = __fmaf_rn(-kf, AG_PIO2_1, x.hi);
+    df r = two_sum(r1, x.lo);
+    r = sub(r, two_prod(kf, AG_PIO2_2));
+    r = add(r, __fmul_rn(-kf, AG_PIO2_3));
+    sincos_core(r, rint_i(__fmul_rn(x.hi, AG_TWO_OVER_PI)), s, c);
+}
+__device__ __forceinline__ df sin_(df x, bool& ok) {
+    df s, c;
+    sincos_(x, &s, &c, ok);
+    return s;
+}
+__device__ __forceinline__ df cos_(df x, bool& ok) {
+    df s, c;
+    sincos_(x, &s, &c, ok);
+    return c;
+}
+// sin(pi v): exact reduction v = q/2 + r, |r| <= 1/4, then sin/cos of pi r.
+__device__ __forceinline__ df sinpi_(df v) {
+    const float qf = rint_f(__fmul_rn(v.hi, 2.0f));
+    const df r = fast_two_sum(__fsub_rn(v.hi, __fmul_rn(qf, 0.5f)), v.lo);
+    df s, c;
+    sincos_core(mul(r, mk(AG_PI_HI, AG_PI_LO)), rint_i(__fmul_rn(v.hi, 2.0f)), &s, &c);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Philox draws as double-floats. Uniform: (2w+1) 2^-33 is exact in a
+// double-float, so uniform(lo, hi) fills with power-of-two ranges are
+// bit-exact. Normal: Box-Muller from the exact 54-bit integers of u and v
+// (random/detail/Backend.h:209-236); log(u) is taken as log(u) for u < 1/2 and
+// as log1p(-(1-u)) above, with 1-u formed in integer arithmetic.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df draw01_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
+    const ag_u32 w = ag::philox_block(seed, g, c).x;
+    return scale(from_u64(2ull * w + 1ull), p2f(-33));
+}
+__device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
+    const ag::q4 x = ag::philox_block(seed, g, c);
+    const ag_u64 z = (ag_u64)x.x ^ ((ag_u64)x.y << 21);
+    const bool lower = z < (1ull << 52);
+    const ag_u64 w = lower ? 2ull * z + 1ull : 2ull * ((1ull << 53) - 1ull - z) + 1ull;
+    const df W = scale(from_u64(w), p2f(-54));
+    const df L = log_s(lower ? 0.0f : 1.0f, lower ? W : neg(W));
+    const df sv = sqrt_(scale(L, -2.0f));
+    // v = V 2^-53 with V = 2 zy + 1 odd; reduce v = q/2 + r exactly in integers
+    // (q = round(2v), r = R 2^-53, |R| <= 2^51) so sin(pi v) keeps full
+    // relative accuracy next to the zeros of the sine.
+    const ag_u64 zy = (ag_u64)x.z ^ ((ag_u64)x.w << 21);
+    const ag_u64 V = 2ull * zy + 1ull;
+    const ag_u64 q = (V + (1ull << 51)) >> 52;
+    const ag_i64 R = (ag_i64)V - (ag_i64)(q << 52);
+    const df ra = scale(from_u64((ag_u64)(R < 0 ? -R : R)), p2f(-53));
+    df s, co;
+    sincos_core(mul(R < 0 ? neg(ra) : ra, mk(AG_PI_HI, AG_PI_LO)), (int)q, &s, &co);
+    return mul(sv, s);
+}
+
+// ---------------------------------------------------------------------------
+// Scalars, simple nodes and the bridge to native FP64 for functions without a
+// double-float kernel (each costs FP64-pipe work, like the native plan).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ df dfc(double x) {   // any double (runtime scalars, literals)
+    const float h = __double2float_rn(x);
+    const float l = isfinite(h) ? __double2float_rn(x - (double)h) : 0.0f;
+    return mk(h, l);
+}
+__device__ __forceinline__ df abs_(df x) { return x.hi < 0.0f ? neg(x) : x; }
+__device__ __forceinline__ df sign_(df x) {
+    return mk(x.hi > 0.0f ? 1.0f : (x.hi < 0.0f ? -1.0f : 0.0f), 0.0f);
+}
+__device__ __forceinline__ df min_(df a, df b) { return lt(b, a) ? b : a; }
+__device__ __forceinline__ df max_(df a, df b) { return gt(b, a) ? b : a; }
+__device__ __forceinline__ double as_d(df x) { return (double)x.hi + (double)x.lo; }
+#define AG_E64_NATIVE1(NAME)                                                                   \
+    __device__ __forceinline__ df nat_##NAME(df x) { return dfc(ag::f_##NAME(as_d(x))); }
+#define AG_E64_NATIVE2(NAME)                                                                   \
+    __device__ __forceinline__ df nat_##NAME(df a, df b) { return dfc(ag::f_##NAME(as_d(a), as_d(b))); }
+AG_E64_NATIVE1(expm1)
+AG_E64_NATIVE1(exp2)
+AG_E64_NATIVE1(log2)
+AG_E64_NATIVE1(log10)
+AG_E64_NATIVE1(tan)
+AG_E64_NATIVE1(asin)
+AG_E64_NATIVE1(acos)
+AG_E64_NATIVE1(atan)
+AG_E64_NATIVE1(tanh)
+AG_E64_NATIVE1(sinh)
+AG_E64_NATIVE1(cosh)
+AG_E64_NATIVE1(floor)
+AG_E64_NATIVE1(ceil)
+AG_E64_NATIVE1(trunc)
+AG_E64_NATIVE1(cbrt)
+AG_E64_NATIVE1(erf)
+AG_E64_NATIVE2(pow)
+AG_E64_NATIVE2(atan2)
+AG_E64_NATIVE2(hypot)
+#undef AG_E64_NATIVE1
+#undef AG_E64_NATIVE2
 
 }  // namespace e64
 }  // namespace ag

@@ -1,0 +1,132 @@
+"""Generate ag_emu64_tables.cuh: the tables and split constants of the
+double-float (float hi + float lo) function kernels in ag_emu64.cuh.
+
+Every value is computed here with mpmath at 200 bits and rounded twice to
+float (hi = fl(v), lo = fl(v - hi)), so hi + lo carries about 48 bits.
+Methods: table-driven exponential (Tang 1989), table-driven logarithm with an
+exact reduction t = m*c - 1 (Tang 1990), sine/cosine by Cody-Waite reduction
+by pi/2 plus a 1/32-spaced table (Cody & Waite 1980).
+
+usage: python aether_gb300/csrc/device/gen_emu64_tables.py
+"""
+
+import os
+
+import mpmath as mp
+import numpy as np
+
+mp.mp.prec = 200
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def f32(v):
+    return float(np.float32(float(v)))
+
+
+def split2(v):
+    hi = f32(v)
+    lo = f32(mp.mpf(v) - hi)
+    return hi, lo
+
+
+def split3(v):
+    hi = f32(v)
+    mid = f32(mp.mpf(v) - hi)
+    lo = f32(mp.mpf(v) - hi - mid)
+    return hi, mid, lo
+
+
+def trunc_bits(v, bits):
+    """v rounded toward zero to `bits` significant bits (a float)."""
+    v = mp.mpf(v)
+    e = mp.floor(mp.log(abs(v), 2))
+    scale = mp.mpf(2) ** (bits - 1 - e)
+    return f32(mp.floor(abs(v) * scale) / scale * mp.sign(v))
+
+
+def fl(x):
+    s = np.float32(x)
+    r = repr(float(s))
+    if "inf" in r or "nan" in r:
+        raise ValueError(r)
+    return "%sf" % np.format_float_scientific(s, precision=9, unique=False)
+
+
+def main():
+    out = ["// generated by gen_emu64_tables.py -- do not edit", "#pragma once", "namespace ag {", "namespace e64 {"]
+
+    # --- exp: 2^(j/64) ----------------------------------------------------
+    exp_hi, exp_lo = zip(*[split2(mp.power(2, mp.mpf(j) / 64)) for j in range(64)])
+    out.append("__device__ const float kExp2TabHi[64] = {%s};" % ", ".join(fl(v) for v in exp_hi))
+    out.append("__device__ const float kExp2TabLo[64] = {%s};" % ", ".join(fl(v) for v in exp_lo))
+    ln2_64 = mp.log(2) / 64
+    # Cody-Waite parts of ln2/64: the first with 11 significant bits so m*C1 is exact for |m| < 2^13.
+    c1 = trunc_bits(ln2_64, 11)
+    c2 = trunc_bits(ln2_64 - c1, 24)
+    c3 = f32(ln2_64 - c1 - c2)
+    out.append("#define AG_LN2_64_1 %s" % fl(c1))
+    out.append("#define AG_LN2_64_2 %s" % fl(c2))
+    out.append("#define AG_LN2_64_3 %s" % fl(c3))
+    out.append("#define AG_INV_LN2_64 %s" % fl(64 / mp.log(2)))
+
+    # --- log: m in [0.75, 1.5), i = round((m-1)*128) in [-32, 64] -----------
+    # c_i ~ 1/m_i as a full float; c_0 = 1 exactly (no cancellation near 1).
+    cs, lh, ll = [], [], []
+    for i in range(-32, 65):
+        if i == 0:
+            c = 1.0
+        else:
+            c = f32(1 / (1 + mp.mpf(i) / 128))
+        cs.append(c)
+        h, l = split2(-mp.log(mp.mpf(c)))
+        lh.append(h)
+        ll.append(l)
+    out.append("__device__ const float kLogC[97] = {%s};" % ", ".join(fl(v) for v in cs))
+    out.append("__device__ const float kLogLHi[97] = {%s};" % ", ".join(fl(v) for v in lh))
+    out.append("__device__ const float kLogLLo[97] = {%s};" % ", ".join(fl(v) for v in ll))
+    # ln2 in three parts: the first with 16 bits so e*LN2_1 is exact for |e| < 2^8.
+    ln2 = mp.log(2)
+    l1 = trunc_bits(ln2, 16)
+    l2 = trunc_bits(ln2 - l1, 24)
+    l3 = f32(ln2 - l1 - l2)
+    out.append("#define AG_LN2_1 %s" % fl(l1))
+    out.append("#define AG_LN2_2 %s" % fl(l2))
+    out.append("#define AG_LN2_3 %s" % fl(l3))
+    t3h, t3l = split2(mp.mpf(1) / 3)
+    out.append("#define AG_THIRD_HI %s" % fl(t3h))
+    out.append("#define AG_THIRD_LO %s" % fl(t3l))
+    t6h, t6l = split2(mp.mpf(1) / 6)
+    out.append("#define AG_SIXTH_HI %s" % fl(t6h))
+    out.append("#define AG_SIXTH_LO %s" % fl(t6l))
+
+    # --- sin/cos at j/32, j in [-26, 26] ------------------------------------
+    sh, sl, ch, cl = [], [], [], []
+    for j in range(-26, 27):
+        a = mp.mpf(j) / 32
+        h, l = split2(mp.sin(a))
+        sh.append(h)
+        sl.append(l)
+        h, l = split2(mp.cos(a))
+        ch.append(h)
+        cl.append(l)
+    for name, vals in (("kSinTabHi", sh), ("kSinTabLo", sl), ("kCosTabHi", ch), ("kCosTabLo", cl)):
+        out.append("__device__ const float %s[53] = {%s};" % (name, ", ".join(fl(v) for v in vals)))
+    # pi/2 in three parts: the first with 12 bits so k*P1 is exact for |k| < 2^12.
+    pio2 = mp.pi / 2
+    p1 = trunc_bits(pio2, 12)
+    p2 = trunc_bits(pio2 - p1, 24)
+    p3 = f32(pio2 - p1 - p2)
+    out.append("#define AG_PIO2_1 %s" % fl(p1))
+    out.append("#define AG_PIO2_2 %s" % fl(p2))
+    out.append("#define AG_PIO2_3 %s" % fl(p3))
+    out.append("#define AG_TWO_OVER_PI %s" % fl(2 / mp.pi))
+    pih, pil = split2(mp.pi)
+    out.append("#define AG_PI_HI %s" % fl(pih))
+    out.append("#define AG_PI_LO %s" % fl(pil))
+    out += ["}  // namespace e64", "}  // namespace ag", ""]
+    with open(os.path.join(HERE, "ag_emu64_tables.cuh"), "w") as f:
+        f.write("\n".join(out))
+
+
+if __name__ == "__main__":
+    main()

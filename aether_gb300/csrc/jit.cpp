@@ -79,10 +79,10 @@ std::unordered_map<uint64_t, std::string> g_mem;
 }  // namespace
 
 std::string compile_for_arch(const std::string& source, const std::string& arch) {
-    const char* hdr_src[] = {kAgDeviceSrc, kAgEmu64Src};
-    const char* hdr_names[] = {"ag_device.cuh", "ag_emu64.cuh"};
+    const char* hdr_src[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc};
+    const char* hdr_names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh"};
     nvrtcProgram prog;
-    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_plan.cu", 2, hdr_src, hdr_names) != NVRTC_SUCCESS)
+    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_plan.cu", 3, hdr_src, hdr_names) != NVRTC_SUCCESS)
         throw std::runtime_error("nvrtcCreateProgram failed");
     const std::string arch_opt = "--gpu-architecture=" + arch;
     const char* opts[] = {arch_opt.c_str(), "--std=c++17", "--fmad=true", "--dopt=on"};
@@ -112,6 +112,7 @@ Compiled compile_cached(const std::string& source, const std::string& tag) {
     h = fnv1a(opts_key, h);
     h = fnv1a(kAgDeviceSrc, h);
     h = fnv1a(kAgEmu64Src, h);
+    h = fnv1a(kAgEmu64TablesSrc, h);
 
     Compiled out;
     out.hash = h;

@@ -385,27 +385,49 @@ struct Gen {
     std::vector<char> done;
     std::ostringstream pro;   // sample-0 prologue (at0 subtrees)
     std::ostringstream body;  // per-lane code
-    int lane_ctx = 0;
+    bool dfm = false;         // double-float working type (emulated FP64)
+    std::string pre = "t";    // variable prefix
 
-    Gen(const Plan& p, const Lowering& l, const std::vector<int>& c) : P(p), L(l), ctx(c), val(p.nodes.size()),
-                                                                         done(p.nodes.size(), 0) {
-        W = P.dst_dtype == DType::F64 ? "double" : "float";
+    Gen(const Plan& p, const Lowering& l, const std::vector<int>& c, bool df_mode = false, std::string prefix = "t")
+        : P(p), L(l), ctx(c), val(p.nodes.size()), done(p.nodes.size(), 0), dfm(df_mode), pre(std::move(prefix)) {
+        W = dfm ? "ag::e64::df" : (P.dst_dtype == DType::F64 ? "double" : "float");
         S = P.dst_dtype == DType::F64 ? "double" : "float";
     }
 
     std::string add(const std::string& a, const std::string& b) const {
+        if (dfm) return "ag::e64::add(" + a + ", " + b + ")";
         return L.contract ? "(" + a + " + " + b + ")" : "ag::rn_add(" + a + ", " + b + ")";
     }
     std::string sub(const std::string& a, const std::string& b) const {
+        if (dfm) return "ag::e64::sub(" + a + ", " + b + ")";
         return L.contract ? "(" + a + " - " + b + ")" : "ag::rn_sub(" + a + ", " + b + ")";
     }
     std::string mul(const std::string& a, const std::string& b) const {
+        if (dfm) return "ag::e64::mul(" + a + ", " + b + ")";
         return L.contract ? "(" + a + " * " + b + ")" : "ag::rn_mul(" + a + ", " + b + ")";
     }
-    std::string div(const std::string& a, const std::string& b) const { return "ag::rn_div(" + a + ", " + b + ")"; }
-    std::string lit(double v) const { return "((" + W + ")" + hexlit(v) + ")"; }
-    std::string fn(const std::string& name) const {
-        return (L.math == 1 && W == "double") ? "ag::e64::f_" + name : "ag::f_" + name;
+    std::string div(const std::string& a, const std::string& b) const {
+        if (dfm) return "ag::e64::div(" + a + ", " + b + ")";
+        return "ag::rn_div(" + a + ", " + b + ")";
+    }
+    std::string neg(const std::string& a) const { return dfm ? "ag::e64::neg(" + a + ")" : "(-" + a + ")"; }
+    std::string lit(double v) const {
+        if (dfm) return "ag::e64::dfc(" + hexlit(v) + ")";
+        return "((" + W + ")" + hexlit(v) + ")";
+    }
+    std::string okv(int id) const { return ctx[size_t(id)] ? "ok0_" : "ok_"; }
+    // Function spelling; `id` selects the range flag for functions that set one.
+    std::string call(const std::string& name, const std::vector<std::string>& args, int id) const {
+        std::string a;
+        for (size_t i = 0; i < args.size(); ++i) a += (i ? ", " : "") + args[i];
+        if (!dfm) return "ag::f_" + name + "(" + a + ")";
+        static const std::set<std::string> own = {"sqrt", "rsqrt", "exp", "log", "log1p", "abs", "sign", "min", "max"};
+        if (name == "sin" || name == "cos") return "ag::e64::" + name + "_(" + a + ", " + okv(id) + ")";
+        if (own.count(name)) return "ag::e64::" + name + "_(" + a + ")";
+        return "ag::e64::nat_" + name + "(" + a + ")";
+    }
+    std::string gtx(const std::string& a, const std::string& b) const {
+        return dfm ? "ag::e64::gt(" + a + ", " + b + ")" : "(" + a + " > " + b + ")";
     }
 
     std::ostringstream& out_for(int id) { return ctx[size_t(id)] ? pro : body; }
@@ -415,7 +437,7 @@ struct Gen {
         std::ostringstream& o = out_for(id);
         std::vector<std::string> names;
         for (size_t c = 0; c < exprs.size(); ++c) {
-            const std::string nm = "t" + std::to_string(id) + "_" + std::to_string(c);
+            const std::string nm = pre + std::to_string(id) + "_" + std::to_string(c);
             o << "        const " << (is_bool ? "bool" : W) << " " << nm << " = " << exprs[c] << ";\n";
             names.push_back(nm);
         }
@@ -431,19 +453,27 @@ struct Gen {
         const std::string& op = n.op;
         const bool c0 = ctx[size_t(id)] != 0;
         std::vector<std::string> e;
-        const std::string lane = c0 ? "0" : "l";
         const std::string gid = c0 ? "g0" : "g";
+        const std::string sid = pre + std::to_string(id);
 
         if (op == "in") {
             const bool pbool = n.dtype == DType::U8;
             for (int c = 0; c < n.comps; ++c) {
                 const std::string src = c0 ? "x" + std::to_string(n.k) + "_0[" + std::to_string(c) + "]"
                                            : "in" + std::to_string(n.k) + "[" + std::to_string(c) + "][l]";
-                e.push_back(pbool ? "(" + src + " != 0)" : "(" + W + ")" + src);
+                if (pbool) {
+                    e.push_back("(" + src + " != 0)");
+                } else if (dfm) {
+                    out_for(id) << "        " << okv(id) << " = " << okv(id) << " && ag::e64::in_range((double)" << src << ");\n";
+                    e.push_back("ag::e64::from_double((double)" + src + ")");
+                } else {
+                    e.push_back("(" + W + ")" + src);
+                }
             }
             def(id, e, pbool);
         } else if (op == "sc") {
-            def(id, {"(" + W + ")a.sc[" + std::to_string(n.k) + "]"});
+            const std::string s = "a.sc[" + std::to_string(n.k) + "]";
+            def(id, {dfm ? "ag::e64::dfc(" + s + ")" : "(" + W + ")" + s});
         } else if (op == "lit") {
             def(id, {lit(n.lit)});
         } else if (op == "bcast") {
@@ -457,8 +487,8 @@ struct Gen {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x = V(0)[size_t(c)];
                 if (op == "sq") e.push_back(mul(x, x));
-                else if (op == "neg") e.push_back("(-" + x + ")");
-                else e.push_back(fn(op) + "(" + x + ")");
+                else if (op == "neg") e.push_back(neg(x));
+                else e.push_back(call(op, {x}, id));
             }
             def(id, e);
         } else if (binary_ops().count(op)) {
@@ -468,7 +498,7 @@ struct Gen {
                 else if (op == "sub") e.push_back(sub(a, b));
                 else if (op == "mul") e.push_back(mul(a, b));
                 else if (op == "div") e.push_back(div(a, b));
-                else e.push_back(fn(op) + "(" + a + ", " + b + ")");
+                else e.push_back(call(op, {a, b}, id));
             }
             def(id, e);
         } else if (op == "scale") {   // CWiseScale: factor * e (expr/nodes/Arithmetic.h:130-140)
@@ -476,18 +506,22 @@ struct Gen {
             def(id, e);
         } else if (op == "mins" || op == "maxs" || op == "pows") {
             const std::string f = op == "mins" ? "min" : op == "maxs" ? "max" : "pow";
-            for (int c = 0; c < n.comps; ++c) e.push_back(fn(f) + "(" + V(0)[size_t(c)] + ", " + V(1)[0] + ")");
+            for (int c = 0; c < n.comps; ++c) e.push_back(call(f, {V(0)[size_t(c)], V(1)[0]}, id));
             def(id, e);
         } else if (op == "clamp") {   // Elementwise.h:138-167
             for (int c = 0; c < n.comps; ++c)
-                e.push_back(fn("min") + "(" + fn("max") + "(" + V(0)[size_t(c)] + ", " + V(1)[0] + "), " + V(2)[0] + ")");
+                e.push_back(call("min", {call("max", {V(0)[size_t(c)], V(1)[0]}, id), V(2)[0]}, id));
             def(id, e);
         } else if (cmp_ops().count(op)) {
             static const std::map<std::string, std::string> sym = {{"gt", ">"}, {"lt", "<"}, {"ge", ">="},
                                                                    {"le", "<="}, {"eq", "=="}, {"ne", "!="},
                                                                    {"and", "&&"}, {"or", "||"}};
-            for (int c = 0; c < n.comps; ++c)
-                e.push_back("(" + V(0)[size_t(c)] + " " + sym.at(op) + " " + V(1)[size_t(c)] + ")");
+            const bool logical = op == "and" || op == "or";
+            for (int c = 0; c < n.comps; ++c) {
+                const std::string a = V(0)[size_t(c)], b = V(1)[size_t(c)];
+                if (dfm && !logical && !K(0).is_bool) e.push_back("ag::e64::" + op + "(" + a + ", " + b + ")");
+                else e.push_back("(" + a + " " + sym.at(op) + " " + b + ")");
+            }
             def(id, e, true);
         } else if (op == "not") {
             for (int c = 0; c < n.comps; ++c) e.push_back("(!" + V(0)[size_t(c)] + ")");
@@ -532,8 +566,8 @@ struct Gen {
             const auto& a = V(0);
             std::string acc = mul(a[0], a[0]);
             for (size_t c = 1; c < a.size(); ++c) acc = add(mul(a[c], a[c]), acc);
-            const std::string rn = "r" + std::to_string(id);
-            out_for(id) << "        const " << W << " " << rn << " = " << div(lit(1.0), fn("sqrt") + "(" + acc + ")") << ";\n";
+            const std::string rn = sid + "r";
+            out_for(id) << "        const " << W << " " << rn << " = " << div(lit(1.0), call("sqrt", {acc}, id)) << ";\n";
             for (size_t c = 0; c < a.size(); ++c) e.push_back(mul(a[c], rn));
             def(id, e);
         } else if (op == "qmul") {   // expr/nodes/Quaternion.h:60-79
@@ -546,12 +580,12 @@ struct Gen {
             def(id, e);
         } else if (op == "qconj") {   // Quaternion.h:103-108
             const auto& a = V(0);
-            e = {a[0], "(-" + a[1] + ")", "(-" + a[2] + ")", "(-" + a[3] + ")"};
+            e = {a[0], neg(a[1]), neg(a[2]), neg(a[3])};
             def(id, e);
         } else if (op == "qrot") {   // Quaternion.h:142-168
             const auto& q = V(0);
             const auto& v = V(1);
-            const std::string t = "q" + std::to_string(id) + "_";
+            const std::string t = sid + "q";
             std::ostringstream& o = out_for(id);
             const std::string two = lit(2.0);
             o << "        const " << W << " " << t << "x = " << mul(two, sub(mul(q[2], v[2]), mul(q[3], v[1]))) << ";\n";
@@ -568,12 +602,16 @@ struct Gen {
         } else if (op == "inv" || op == "det") {   // expr/nodes/Inverse.h:73-118, Expression.h:400-428
             const auto& m = V(0);
             const int dim = K(0).shape[0];
-            const std::string d = "det" + std::to_string(id);
+            const std::string d = sid + "det";
             std::ostringstream& o = out_for(id);
+            // Emulated FP64 divides by the determinant once, as a reciprocal.
+            const std::string rd = sid + "rdet";
+            auto q = [&](const std::string& num) { return dfm ? mul(num, rd) : div(num, d); };
             if (dim == 2) {
                 o << "        const " << W << " " << d << " = " << sub(mul(m[0], m[3]), mul(m[1], m[2])) << ";\n";
+                if (dfm && op == "inv") o << "        const " << W << " " << rd << " = ag::e64::recip(" << d << ");\n";
                 if (op == "det") e = {d};
-                else e = {div(m[3], d), div("(-" + m[1] + ")", d), div("(-" + m[2] + ")", d), div(m[0], d)};
+                else e = {q(m[3]), q(neg(m[1])), q(neg(m[2])), q(m[0])};
             } else {
                 const std::string &a = m[0], &b = m[1], &c = m[2], &dd = m[3], &ee = m[4], &f = m[5], &g = m[6],
                                   &h = m[7], &k = m[8];
@@ -581,14 +619,13 @@ struct Gen {
                   << add(sub(mul(a, sub(mul(ee, k), mul(f, h))), mul(b, sub(mul(dd, k), mul(f, g)))),
                          mul(c, sub(mul(dd, h), mul(ee, g))))
                   << ";\n";
+                if (dfm && op == "inv") o << "        const " << W << " " << rd << " = ag::e64::recip(" << d << ");\n";
                 if (op == "det") {
                     e = {d};
                 } else {
-                    e = {div(sub(mul(ee, k), mul(f, h)), d), div(sub(mul(c, h), mul(b, k)), d),
-                         div(sub(mul(b, f), mul(c, ee)), d), div(sub(mul(f, g), mul(dd, k)), d),
-                         div(sub(mul(a, k), mul(c, g)), d), div(sub(mul(c, dd), mul(a, f)), d),
-                         div(sub(mul(dd, h), mul(ee, g)), d), div(sub(mul(b, g), mul(a, h)), d),
-                         div(sub(mul(a, ee), mul(b, dd)), d)};
+                    e = {q(sub(mul(ee, k), mul(f, h))), q(sub(mul(c, h), mul(b, k))), q(sub(mul(b, f), mul(c, ee))),
+                         q(sub(mul(f, g), mul(dd, k))), q(sub(mul(a, k), mul(c, g))), q(sub(mul(c, dd), mul(a, f))),
+                         q(sub(mul(dd, h), mul(ee, g))), q(sub(mul(b, g), mul(a, h))), q(sub(mul(a, ee), mul(b, dd)))};
                 }
             }
             def(id, e);
@@ -629,43 +666,52 @@ struct Gen {
             auto term = [&](int c) -> std::string {
                 if (op == "dot") return mul(a[size_t(c)], V(1)[size_t(c)]);
                 if (op == "sum") return a[size_t(c)];
-                if (op == "maxnorm") return fn("abs") + "(" + a[size_t(c)] + ")";
+                if (op == "maxnorm") return call("abs", {a[size_t(c)]}, id);
                 return mul(a[size_t(c)], a[size_t(c)]);
             };
             std::string acc = term(0);
             for (int c = 1; c < m; ++c) {
                 const std::string t = term(c);
-                acc = op == "maxnorm" ? "((" + t + ") > (" + acc + ") ? (" + t + ") : (" + acc + "))" : add(t, acc);
+                acc = op == "maxnorm" ? "(" + gtx(t, acc) + " ? (" + t + ") : (" + acc + "))" : add(t, acc);
             }
-            if (op == "norm") acc = fn("sqrt") + "(" + acc + ")";
-            if (op == "rnorm") acc = div(lit(1.0), fn("sqrt") + "(" + acc + ")");
+            if (op == "norm") acc = call("sqrt", {acc}, id);
+            if (op == "rnorm") acc = div(lit(1.0), call("sqrt", {acc}, id));
             def(id, {acc});
         } else if (op == "uniform" || op == "normal" || op == "lognormal" || op == "exponential" || op == "bernoulli") {
             const std::string key = "a.key[" + std::to_string(n.k) + "]";
             const bool b0 = K(0).shape.empty();
             const bool b1 = n.kids.size() > 1 && K(1).shape.empty();
             const std::string wp = "(" + W + "*)0";
+            auto u01 = [&](const char* salt, const std::string& cc) {
+                return dfm ? "ag::e64::draw01_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
+                           : "ag::draw01(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
+            };
+            auto nrm = [&](const char* salt, const std::string& cc) {
+                return dfm ? "ag::e64::normal_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
+                           : "ag::drawn(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
+            };
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x0 = V(0)[b0 ? 0 : size_t(c)];
                 const std::string x1 = n.kids.size() > 1 ? V(1)[b1 ? 0 : size_t(c)] : "";
                 const std::string cc = std::to_string(c) + "u";
                 if (op == "uniform") {   // DistributionLeaf.h:125-131
-                    e.push_back(add(x0, mul(sub(x1, x0), "ag::draw01(" + wp + ", " + key + " ^ AG_SALT_UNIFORM, " + gid + ", " + cc + ")")));
+                    e.push_back(add(x0, mul(sub(x1, x0), u01("AG_SALT_UNIFORM", cc))));
                 } else if (op == "normal") {   // DistributionLeaf.h:192-199
-                    e.push_back(add(x0, mul(x1, "ag::drawn(" + wp + ", " + key + " ^ AG_SALT_NORMAL, " + gid + ", " + cc + ")")));
+                    e.push_back(add(x0, mul(x1, nrm("AG_SALT_NORMAL", cc))));
                 } else if (op == "lognormal") {   // DistributionLeaf.h:257-264
-                    e.push_back(fn("exp") + "(" + add(x0, mul(x1, "ag::drawn(" + wp + ", " + key + " ^ AG_SALT_LOGNORMAL, " + gid + ", " + cc + ")")) + ")");
+                    e.push_back(call("exp", {add(x0, mul(x1, nrm("AG_SALT_LOGNORMAL", cc)))}, id));
                 } else if (op == "exponential") {   // DistributionLeaf.h:329-333
-                    e.push_back(div("(-" + fn("log") + "(ag::draw01(" + wp + ", " + key + " ^ AG_SALT_EXPONENTIAL, " + gid + ", " + cc + ")))", x0));
+                    e.push_back(div(neg(call("log", {u01("AG_SALT_EXPONENTIAL", cc)}, id)), x0));
                 } else {   // DistributionLeaf.h:380-385
-                    e.push_back("(ag::draw01(" + wp + ", " + key + " ^ AG_SALT_BERNOULLI, " + gid + ", " + cc + ") < " + x0 + " ? " + lit(1.0) + " : " + lit(0.0) + ")");
+                    const std::string u = u01("AG_SALT_BERNOULLI", cc);
+                    e.push_back("(" + (dfm ? "ag::e64::lt(" + u + ", " + x0 + ")" : "(" + u + " < " + x0 + ")") + " ? " +
+                                lit(1.0) + " : " + lit(0.0) + ")");
                 }
             }
             def(id, e);
         } else {
             fail("no generator for '" + op + "'");
         }
-        (void)lane;
         done[size_t(id)] = 1;
         return val[size_t(id)];
     }
@@ -696,7 +742,19 @@ int effective_vec(const Plan& plan, const Lowering& low) {
     return widest >= 8 ? 2 : 4;
 }
 
-std::string generate_source(const Plan& plan_in, const Lowering& low) {
+std::string kernel_base(const Plan& plan, const std::string& text) {
+    uint64_t h = 1469598103934665603ULL;
+    for (unsigned char c : text) {
+        h ^= c;
+        h *= 1099511628211ULL;
+    }
+    char buf[64];
+    const char* kind = plan.wants_sum() ? "sum" : (plan.has_random && plan.n_operands == 0) ? "fill" : "expr";
+    std::snprintf(buf, sizeof buf, "ag_%s_%08x", kind, unsigned(h ^ (h >> 32)));
+    return buf;
+}
+
+std::string generate_source(const Plan& plan_in, const Lowering& low, const std::string& base) {
     // Re-derive the sample contexts (at0 subtrees) from the node graph: every
     // node reachable only through `at0` belongs to the sample-0 prologue.
     const Plan& P = plan_in;
@@ -716,8 +774,16 @@ std::string generate_source(const Plan& plan_in, const Lowering& low) {
         // A node used both inside and outside at0 would need two copies; the
         // parser keys its memo by context, so such nodes are already distinct.
     }
-    Gen g(P, low, ctx);
-    const std::vector<std::string>& root = g.emit(P.root);
+    // Emulated FP64: the tree is generated twice, once in double-float (the
+    // fast path) and once on the native FP64 pipe (the per-lane fallback).
+    const bool emu = low.math == 1 && P.dst_dtype == DType::F64;
+    Gen g(P, low, ctx, emu, emu ? "d" : "t");
+    const std::vector<std::string> root = g.emit(P.root);
+    Lowering nat = low;
+    nat.math = 0;
+    Gen gn(P, nat, ctx, false, "n");
+    std::vector<std::string> nroot;
+    if (emu) nroot = gn.emit(P.root);
 
     const int vec = effective_vec(P, low);
     std::ostringstream o;
@@ -767,21 +833,40 @@ std::string generate_source(const Plan& plan_in, const Lowering& low) {
           << "])[c * a.pitch[" << k << "]];\n";
     }
     if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n";
+    if (emu) o << "    bool ok0_ = true;\n";
     o << g.pro.str();
+    if (emu) o << gn.pro.str();
     if (store) o << "    " << S << " out[" << P.dst_comps << "][L];\n";
     o << "#pragma unroll\n    for (int l = 0; l < L; ++l) {\n";
     if (P.has_random) o << "        const ag_u32 g = a.offset + (ag_u32)(s0[l / VEC] + (ag_u64)(l % VEC));\n";
+    if (emu) o << "        bool ok_ = ok0_;\n";
     o << g.body.str();
+    // Final working values of the output components.
+    const std::string FW = emu ? "double" : W;
     for (int c = 0; c < P.dst_comps; ++c) {
-        const std::string v = root[size_t(c)];
+        if (emu) {
+            o << "        double fv" << c << " = ag::e64::to_double(" << root[size_t(c)] << ");\n";
+            o << "        ok_ = ok_ && ag::e64::out_ok(" << root[size_t(c)] << ");\n";
+        } else {
+            o << "        const " << W << " fv" << c << " = " << root[size_t(c)] << ";\n";
+        }
+    }
+    if (emu) {
+        // Samples outside the double-float range are recomputed natively.
+        o << "        if (!ok_) {\n" << gn.body.str();
+        for (int c = 0; c < P.dst_comps; ++c) o << "            fv" << c << " = " << nroot[size_t(c)] << ";\n";
+        o << "        }\n";
+    }
+    for (int c = 0; c < P.dst_comps; ++c) {
+        const std::string v = "fv" + std::to_string(c);
         if (store) {
             if (P.op == "set" || P.op == "setsum") o << "        out[" << c << "][l] = (" << S << ")" << v << ";\n";
-            else if (P.op == "add") o << "        out[" << c << "][l] = (" << S << ")ag::rn_add((" << W << ")cur[" << c << "][l], " << v << ");\n";
-            else o << "        out[" << c << "][l] = (" << S << ")ag::rn_sub((" << W << ")cur[" << c << "][l], " << v << ");\n";
+            else if (P.op == "add") o << "        out[" << c << "][l] = (" << S << ")ag::rn_add((" << FW << ")cur[" << c << "][l], " << v << ");\n";
+            else o << "        out[" << c << "][l] = (" << S << ")ag::rn_sub((" << FW << ")cur[" << c << "][l], " << v << ");\n";
         }
     }
     if (sum) {
-        o << "        if (s0[l / VEC] + (ag_u64)(l % VEC) < a.n) ag::neumaier_add(acc_h, acc_c, (double)(" << root[0] << "));\n";
+        o << "        if (s0[l / VEC] + (ag_u64)(l % VEC) < a.n) ag::neumaier_add(acc_h, acc_c, (double)fv0);\n";
     }
     o << "    }\n";
     if (store) {
@@ -796,7 +881,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low) {
     const std::string lb = low.min_blocks > 0 ? "__launch_bounds__(AG_BLOCK, " + std::to_string(low.min_blocks) + ")"
                                               : "__launch_bounds__(AG_BLOCK)";
     for (int variant = 0; variant < 2; ++variant) {
-        const std::string name = variant == 0 ? "ag_plan_v" : "ag_plan_s";
+        const std::string name = base + (variant == 0 ? "_v" : "_s");
         const std::string V = variant == 0 ? "AG_VEC" : "1";
         k << "extern \"C\" __global__ void " << lb << " " << name << "(const AgArgs a) {\n";
         k << "    const ag_u64 per = (ag_u64)AG_BLOCK * AG_IPT * " << V << ";\n";

@@ -58,9 +58,13 @@ Plan parse_plan(const std::string& text);
 const char* dtype_name(DType d);
 int dtype_size(DType d);
 
-// Generated CUDA source for the plan: kernels `ag_plan_v` (vectorized lane
-// groups) and `ag_plan_s` (one sample per lane group).
-std::string generate_source(const Plan& plan, const Lowering& low);
+// Generated CUDA source for the plan: kernels `<base>_v` (vectorized lane
+// groups) and `<base>_s` (one sample per lane group).
+std::string generate_source(const Plan& plan, const Lowering& low, const std::string& base = "ag_plan");
+
+// Kernel base name of a plan: ag_<expr|fill|sum>_<8 hex digits of the text hash>,
+// so profiles and launch lists tell plans apart.
+std::string kernel_base(const Plan& plan, const std::string& text);
 
 // Chunk = samples one CTA covers per pass = block * ipt * vec.
 int effective_vec(const Plan& plan, const Lowering& low);

@@ -309,7 +309,12 @@ def main():
     ap.add_argument("--math", type=int, default=0, help="0 native FP64, 1 emulated FP64")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
+    ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
     args = ap.parse_args()
+    global N_EXPR, N_FILL, BYTES_EXPR, BYTES_FILL
+    N_EXPR, N_FILL = 1 << args.expr_log2, 1 << args.fill_log2
+    BYTES_EXPR, BYTES_FILL = N_EXPR * 120, N_FILL * 8
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

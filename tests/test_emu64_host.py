@@ -1,0 +1,43 @@
+"""The double-float kernels of the emulated FP64 mode (ag_emu64.cuh), built as
+host C++ through tests/emu_host/host_shim.h and checked against long double.
+Errors are in units of 2^-53 relative (double ulps at the bottom of a binade).
+
+Bounds hold for well-conditioned uses; where a function is ill-conditioned
+with respect to a relative perturbation of its input (log near 1, exp at large
+|x|, sums that cancel), the error is the 2^-48 input rounding of a
+double-float times that condition number, and the GPU tests check those
+expressions against the magnitude of their terms."""
+
+import json
+import os
+import subprocess
+
+import pytest
+
+from conftest import REPO
+
+BOUNDS = {
+    "roundtrip": 33, "sqrt": 256, "rsqrt": 256, "exp_small": 128, "log1p": 128, "log1p_tiny": 160,
+    "log1p_neg": 1024, "sin": 160, "cos": 160, "recip": 192, "mul": 192, "div": 192, "cfg2a": 256,
+    "cfg1_termscale": 160, "normal_abs_rel": 256,
+}
+
+
+@pytest.fixture(scope="module")
+def emu_report(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("emu") / "emu_check")
+    src = os.path.join(REPO, "tests", "emu_host", "emu_check.cpp")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-o", exe, src])
+    return json.loads(subprocess.check_output([exe]))
+
+
+@pytest.mark.parametrize("name", sorted(BOUNDS))
+def test_emulated_function_error_bounds(emu_report, name):
+    r = emu_report[name]
+    assert r["n"] > 100000 and r["bad"] == 0
+    assert r["max"] <= BOUNDS[name], (name, r)
+
+
+def test_normals_inside_the_reference_tolerance(emu_report):
+    # random/detail/Backend.h:44-51: abs+rel 1e-12 for double normals.
+    assert emu_report["normal_abs_rel"]["max"] * 2.0 ** -53 < 1e-12
