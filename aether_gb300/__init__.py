@@ -171,10 +171,33 @@ class Launch:
         _abi.check(_abi.lib().aether_plan_launch(self.plan.handle, ctypes.byref(self.args), ctypes.c_void_p(s)))
 
 
-def prepare(dst, expr, op="set", n=None, sample_offset=0, reduce_out=None, workspace=None, **low):
-    """Lower `dst <op>= expr` and bind its arguments; returns a Launch."""
+def prepare(dst, expr, op="set", n=None, sample_offset=0, reduce_out=None, workspace=None, tune=False, **low):
+    """Lower `dst <op>= expr` and bind its arguments; returns a Launch.
+
+    tune=True takes the autotuned lowering of this plan on this device (see
+    tune.py), timing the candidates first if none is cached. Only plans that
+    overwrite their destination are tuned (set/sum/setsum)."""
     if isinstance(expr, (int, float)):
         expr = constant(expr, dst.shape)
+    if tune and op in ("set", "sum", "setsum"):
+        from . import tune as _tune
+        ctx = IrContext()
+        if op == "sum":
+            dtype, shape = dst if isinstance(dst, tuple) else ("f64", ())
+        else:
+            dtype, shape = dst.dtype, (dst.shape if dst.shape != (1,) or expr.shape == (1,) else ())
+        ir = plan_text(dtype, shape, op, expr, ctx)
+        math, contract = low.get("math", 0), low.get("contract", -1)
+        best = _tune.tuned(ir, math, contract)
+        if best is None:
+            base = {k: v for k, v in low.items() if k in ("math", "contract")}
+
+            def make(**cand):
+                return prepare(dst, expr, op=op, n=n, sample_offset=sample_offset, reduce_out=reduce_out,
+                               workspace=workspace, **base, **cand)
+            best, _ = _tune.tune(make, ir, math, contract)
+        low = dict(low)
+        low.update(best)
     ctx = IrContext()
     if op in ("sum",):
         dtype, shape = dst if isinstance(dst, tuple) else ("f64", ())

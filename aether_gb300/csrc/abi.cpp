@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -113,12 +114,14 @@ struct AgArgsHost {
     const char* ops[16];
     uint64_t pitch[16];
     double sc[16];
+    float sch[16];
+    float scl[16];
     uint64_t key[8];
     double* red;
     char* ws;
     uint64_t ws_bytes;
 };
-static_assert(sizeof(AgArgsHost) == 504, "AgArgs layout");
+static_assert(sizeof(AgArgsHost) == 632, "AgArgs layout");
 
 struct PlanObj {
     ag::Plan plan;
@@ -428,7 +431,11 @@ AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream
             const int es = ag::dtype_size(pl.operand_dtype[size_t(i)]);
             aligned = aligned && (reinterpret_cast<uintptr_t>(o.ptr) % 16 == 0) && (comps == 1 || (pitch * es) % 16 == 0);
         }
-        for (int i = 0; i < pl.n_scalars; ++i) k.sc[i] = a->scalars[i];
+        for (int i = 0; i < pl.n_scalars; ++i) {
+            k.sc[i] = a->scalars[i];
+            k.sch[i] = float(a->scalars[i]);
+            k.scl[i] = std::isfinite(k.sch[i]) ? float(a->scalars[i] - double(k.sch[i])) : 0.0f;
+        }
         for (int i = 0; i < pl.n_keys; ++i) k.key[i] = a->keys[i];
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         const bool vect = aligned && P->vec > 1;

@@ -28,12 +28,14 @@ struct AgArgs {
     const char* ops[AG_MAX_OPS];  // plane 0 of each operand
     ag_u64 pitch[AG_MAX_OPS];
     double sc[AG_MAX_SC];         // runtime scalars
+    float sch[AG_MAX_SC];         // the same scalars split as double-float (hi, lo) pairs,
+    float scl[AG_MAX_SC];         // for plans lowered to emulated FP64
     ag_u64 key[AG_MAX_KEYS];      // generator keys of random leaves
     double* red;                  // sum plans: (hi, comp) result
     char* ws;                     // sum plans: counter + per-chunk partials
     ag_u64 ws_bytes;
 };
-static_assert(sizeof(AgArgs) == 504, "AgArgs layout must match the host image in abi.cpp");
+static_assert(sizeof(AgArgs) == 632, "AgArgs layout must match the host image in abi.cpp");
 
 namespace ag {
 

@@ -170,7 +170,9 @@ __device__ __forceinline__ df from_double(double x) {
     const unsigned hb = ((((h32 & 0x7fffffffu) - (896u << 20)) << 3) | (l32 >> 29)) | sign;
     // lo: the remaining 29 bits, rounded to a float and scaled by 2^(ex-1075)
     const float lo = __fmul_rn(__uint2float_rn(l32 & 0x1fffffffu), __int_as_float((ex - 948) << 23));
-    return fast_two_sum(__int_as_float(hb), __int_as_float(__float_as_int(lo) ^ sign));
+    // hi + lo is the double to 2^-48; |lo| < ulp(hi) already, so the pair is
+    // used without renormalising.
+    return mk(__int_as_float(hb), __int_as_float(__float_as_int(lo) ^ sign));
 }
 // A normal float (or zero) as a double.
 __device__ __forceinline__ double f2d(float f) {
@@ -257,15 +259,14 @@ __device__ __forceinline__ df exp_(df x) {
 // log_s(s, x) is log(s + x) for s in {0, 1}: log for s = 0, log1p for s = 1,
 // with t formed from s and x separately so 1 + x is never rounded.
 // ---------------------------------------------------------------------------
+// log(1+t) for |t| <= 2^-10.6: t - t^2/2 in double-float, the rest
+// t^2 (t/3 - t^2/4 + t^3/5) in float (at most 2^-47.6 relative to t).
 __device__ __forceinline__ df log1p_poly(df t) {
     const df t2 = sqr(t);
-    const df t3 = mul(t2, t);
     const float th = t.hi;
-    const float t4 = __fmul_rn(__fmul_rn(th, th), __fmul_rn(th, th));
-    const float tail = __fmul_rn(t4, __fmaf_rn(th, __fmaf_rn(th, __fmaf_rn(th, 0.142857143f, -0.166666667f), 0.2f), -0.25f));
-    df q = add(mul(t3, mk(AG_THIRD_HI, AG_THIRD_LO)), tail);
-    q = add_fast(scale(t2, -0.5f), q);
-    return add_fast(t, q);
+    const float q = __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, 0.2f, -0.25f), 0.333333333f));
+    const df s = add_fast(t, scale(t2, -0.5f));
+    return add(s, __fmul_rn(t2.hi, q));
 }
 __device__ __forceinline__ df log_s(float s, df x) {
     const float yh = __fadd_rn(s, x.hi);
@@ -277,18 +278,20 @@ __device__ __forceinline__ df log_s(float s, df x) {
         e += 1;
     }
     const float m = __int_as_float(mb);
-    const int i = rint_i(__fmul_rn(__fsub_rn(m, 1.0f), 128.0f));
-    const float c = __ldg(&kLogC[i + 32]);
+    const int i = rint_i(__fmul_rn(__fsub_rn(m, 1.0f), 1024.0f)) + AG_LOG_TAB_OFF;
+    const float c = __ldg(&kLogC[i]);
     const float A = __fmul_rn(c, p2f(-e));         // c 2^-e, exact
     const df B = two_sum(__fmul_rn(s, A), -1.0f);   // s A - 1, exact
     const df C = mul(x, A);
     const df t = add(B, C);
     const df lp = log1p_poly(t);
-    const df L = mk(__ldg(&kLogLHi[i + 32]), __ldg(&kLogLLo[i + 32]));
+    const df L = mk(__ldg(&kLogLHi[i]), __ldg(&kLogLLo[i]));
     const float fe = (float)e;
     const df p2 = two_prod(fe, AG_LN2_2);
     const df E = add(fast_two_sum(__fmul_rn(fe, AG_LN2_1), p2.hi), __fmaf_rn(fe, AG_LN2_3, p2.lo));
-    const df res = add(E, add(L, lp));
+    // |lp| < |L| except for i == 0 (L = 0), and e ln2 + L cancels by at most a
+    // factor 2.4, so the sums need no cancellation-safe form.
+    const df res = add_fast(E, add_fast(L, lp));
     const bool valid = yh > 0.0f && e > -120 && e < 120;
     return valid ? res : mk(__int_as_float(0x7fc00000), 0.0f);
 }
@@ -299,9 +302,13 @@ __device__ __forceinline__ df log1p_(df x) { return log_s(1.0f, x); }
 // sin/cos: r in [-pi/4, pi/4] split as r = j/32 + t (|t| <= 1/64);
 // sin r = S_j + S_j (cos t - 1) + C_j sin t, cos r = C_j + C_j (cos t - 1) - S_j sin t.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void sincos_core(df r, int q, df* so, df* co) {
+// One output of sin/cos at x = q pi/2 + r: sin x is +-sin r or +-cos r by
+// quadrant, and both are A + A (cos t - 1) + B sin t with the table pair
+// (A, B) = (S_j, C_j) for sin r and (C_j, -S_j) for cos r, so only the
+// wanted one is evaluated.
+__device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
     const float jf = rint_f(__fmul_rn(r.hi, 32.0f));
-    const int j = rint_i(__fmul_rn(r.hi, 32.0f));
+    const int j = rint_i(__fmul_rn(r.hi, 32.0f)) + 26;
     const df t = fast_two_sum(__fsub_rn(r.hi, __fmul_rn(jf, 0.03125f)), r.lo);
     const df t2 = sqr(t);
     const float th = t.hi;
@@ -313,43 +320,32 @@ __device__ __forceinline__ void sincos_core(df r, int q, df* so, df* co) {
     // cos t - 1 = -t^2/2 + t^4/24 - t^6/720
     const float c4 = __fmul_rn(__fmul_rn(th2, th2), __fmaf_rn(th2, -1.38888889e-3f, 4.16666667e-2f));
     const df cm1 = add(scale(t2, -0.5f), c4);
-    const df S = mk(__ldg(&kSinTabHi[j + 26]), __ldg(&kSinTabLo[j + 26]));
-    const df C = mk(__ldg(&kCosTabHi[j + 26]), __ldg(&kCosTabLo[j + 26]));
-    const df sr = add(add(S, mul(S, cm1)), mul(C, st));
-    const df cr = sub(add(C, mul(C, cm1)), mul(S, st));
-    const int qq = q & 3;
-    const df s0 = (qq & 1) ? cr : sr;
-    const df c0 = (qq & 1) ? sr : cr;
-    *so = (qq & 2) ? neg(s0) : s0;
-    *co = ((qq + 1) & 2) ? neg(c0) : c0;
+    const int qq = (q + (want_cos ? 1 : 0)) & 3;   // cos x = sin(x + pi/2)
+    const bool odd = qq & 1;
+    const df S = mk(__ldg(&kSinTabHi[j]), __ldg(&kSinTabLo[j]));
+    const df C = mk(__ldg(&kCosTabHi[j]), __ldg(&kCosTabLo[j]));
+    const df A = odd ? C : S;
+    const df B = odd ? neg(S) : C;
+    const df v = add(add(A, mul(A, cm1)), mul(B, st));
+    return (qq & 2) ? neg(v) : v;
 }
 // Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.
-__device__ __forceinline__ void sincos_(df x, df* s, df* c, bool& ok) {
+__device__ __forceinline__ df trig_(df x, bool want_cos, bool& ok) {
     ok = ok && fabsf(x.hi) < 6000.0f;
     const float kf = rint_f(__fmul_rn(x.hi, AG_TWO_OVER_PI));
     const float r1 = __fmaf_rn(-kf, AG_PIO2_1, x.hi);
     df r = two_sum(r1, x.lo);
     r = sub(r, two_prod(kf, AG_PIO2_2));
     r = add(r, __fmul_rn(-kf, AG_PIO2_3));
-    sincos_core(r, rint_i(__fmul_rn(x.hi, AG_TWO_OVER_PI)), s, c);
+    return trig_core(r, rint_i(__fmul_rn(x.hi, AG_TWO_OVER_PI)), want_cos);
 }
-__device__ __forceinline__ df sin_(df x, bool& ok) {
-    df s, c;
-    sincos_(x, &s, &c, ok);
-    return s;
-}
-__device__ __forceinline__ df cos_(df x, bool& ok) {
-    df s, c;
-    sincos_(x, &s, &c, ok);
-    return c;
-}
+__device__ __forceinline__ df sin_(df x, bool& ok) { return trig_(x, false, ok); }
+__device__ __forceinline__ df cos_(df x, bool& ok) { return trig_(x, true, ok); }
 // sin(pi v): exact reduction v = q/2 + r, |r| <= 1/4, then sin/cos of pi r.
 __device__ __forceinline__ df sinpi_(df v) {
     const float qf = rint_f(__fmul_rn(v.hi, 2.0f));
     const df r = fast_two_sum(__fsub_rn(v.hi, __fmul_rn(qf, 0.5f)), v.lo);
-    df s, c;
-    sincos_core(mul(r, mk(AG_PI_HI, AG_PI_LO)), rint_i(__fmul_rn(v.hi, 2.0f)), &s, &c);
-    return s;
+    return trig_core(mul(r, mk(AG_PI_HI, AG_PI_LO)), rint_i(__fmul_rn(v.hi, 2.0f)), false);
 }
 
 // ---------------------------------------------------------------------------
@@ -379,9 +375,7 @@ __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag_u64 q = (V + (1ull << 51)) >> 52;
     const ag_i64 R = (ag_i64)V - (ag_i64)(q << 52);
     const df ra = scale(from_u64((ag_u64)(R < 0 ? -R : R)), p2f(-53));
-    df s, co;
-    sincos_core(mul(R < 0 ? neg(ra) : ra, mk(AG_PI_HI, AG_PI_LO)), (int)q, &s, &co);
-    return mul(sv, s);
+    return mul(sv, trig_core(mul(R < 0 ? neg(ra) : ra, mk(AG_PI_HI, AG_PI_LO)), (int)q, false));
 }
 
 // ---------------------------------------------------------------------------

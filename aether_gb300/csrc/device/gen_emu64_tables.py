@@ -69,21 +69,23 @@ def main():
     out.append("#define AG_LN2_64_3 %s" % fl(c3))
     out.append("#define AG_INV_LN2_64 %s" % fl(64 / mp.log(2)))
 
-    # --- log: m in [0.75, 1.5), i = round((m-1)*128) in [-32, 64] -----------
+    # --- log: m in [0.75, 1.5), i = round((m-1)*1024) in [-256, 512] --------
     # c_i ~ 1/m_i as a full float; c_0 = 1 exactly (no cancellation near 1).
+    # |t| = |m c_i - 1| <= 2^-10.6, so log(1+t) needs only t - t^2/2 exactly.
     cs, lh, ll = [], [], []
-    for i in range(-32, 65):
+    for i in range(-256, 513):
         if i == 0:
             c = 1.0
         else:
-            c = f32(1 / (1 + mp.mpf(i) / 128))
+            c = f32(1 / (1 + mp.mpf(i) / 1024))
         cs.append(c)
         h, l = split2(-mp.log(mp.mpf(c)))
         lh.append(h)
         ll.append(l)
-    out.append("__device__ const float kLogC[97] = {%s};" % ", ".join(fl(v) for v in cs))
-    out.append("__device__ const float kLogLHi[97] = {%s};" % ", ".join(fl(v) for v in lh))
-    out.append("__device__ const float kLogLLo[97] = {%s};" % ", ".join(fl(v) for v in ll))
+    out.append("#define AG_LOG_TAB_OFF 256")
+    out.append("__device__ const float kLogC[769] = {%s};" % ", ".join(fl(v) for v in cs))
+    out.append("__device__ const float kLogLHi[769] = {%s};" % ", ".join(fl(v) for v in lh))
+    out.append("__device__ const float kLogLLo[769] = {%s};" % ", ".join(fl(v) for v in ll))
     # ln2 in three parts: the first with 16 bits so e*LN2_1 is exact for |e| < 2^8.
     ln2 = mp.log(2)
     l1 = trunc_bits(ln2, 16)

@@ -375,6 +375,15 @@ std::string hexlit(double v) {
     return buf;
 }
 
+std::string ctype_of(DType d) {
+    switch (d) {
+    case DType::F64: return "double";
+    case DType::I32: return "int";
+    case DType::U8: return "unsigned char";
+    default: return "float";
+    }
+}
+
 struct Gen {
     const Plan& P;
     const Lowering& L;
@@ -387,6 +396,29 @@ struct Gen {
     std::ostringstream body;  // per-lane code
     bool dfm = false;         // double-float working type (emulated FP64)
     std::string pre = "t";    // variable prefix
+    bool direct = false;      // leaves load their own sample `s` (per-lane fallback function)
+    std::vector<signed char> nn_memo;
+
+    // Conservative sign analysis: true when node `id` can never be negative,
+    // which lets emulated sums skip the cancellation-safe form.
+    bool nonneg(int id) {
+        if (nn_memo.empty()) nn_memo.assign(P.nodes.size(), -1);
+        signed char& m = nn_memo[size_t(id)];
+        if (m >= 0) return m != 0;
+        const Node& n = P.nodes[size_t(id)];
+        const std::string& op = n.op;
+        bool r = false;
+        if (op == "sq" || op == "abs" || op == "sqrt" || op == "rsqrt" || op == "exp" || op == "norm" ||
+            op == "sqnorm" || op == "rnorm" || op == "exp2" || op == "cosh")
+            r = true;
+        else if (op == "lit") r = n.lit >= 0.0;
+        else if (op == "bcast" || op == "at0") r = nonneg(n.kids[0]);
+        else if (op == "mul") r = n.kids[0] == n.kids[1] || (nonneg(n.kids[0]) && nonneg(n.kids[1]));
+        else if (op == "add" || op == "scale") r = nonneg(n.kids[0]) && nonneg(n.kids[1]);
+        else if (op == "log1p") r = nonneg(n.kids[0]);
+        m = r ? 1 : 0;
+        return r;
+    }
 
     Gen(const Plan& p, const Lowering& l, const std::vector<int>& c, bool df_mode = false, std::string prefix = "t")
         : P(p), L(l), ctx(c), val(p.nodes.size()), done(p.nodes.size(), 0), dfm(df_mode), pre(std::move(prefix)) {
@@ -459,8 +491,11 @@ struct Gen {
         if (op == "in") {
             const bool pbool = n.dtype == DType::U8;
             for (int c = 0; c < n.comps; ++c) {
-                const std::string src = c0 ? "x" + std::to_string(n.k) + "_0[" + std::to_string(c) + "]"
-                                           : "in" + std::to_string(n.k) + "[" + std::to_string(c) + "][l]";
+                std::string src = c0 ? "x" + std::to_string(n.k) + "_0[" + std::to_string(c) + "]"
+                                     : "in" + std::to_string(n.k) + "[" + std::to_string(c) + "][l]";
+                if (direct)
+                    src = "((const " + ctype_of(n.dtype) + "*)a.ops[" + std::to_string(n.k) + "])[(ag_u64)" +
+                          std::to_string(c) + " * a.pitch[" + std::to_string(n.k) + "] + " + (c0 ? "0" : "s") + "]";
                 if (pbool) {
                     e.push_back("(" + src + " != 0)");
                 } else if (dfm) {
@@ -473,7 +508,8 @@ struct Gen {
             def(id, e, pbool);
         } else if (op == "sc") {
             const std::string s = "a.sc[" + std::to_string(n.k) + "]";
-            def(id, {dfm ? "ag::e64::dfc(" + s + ")" : "(" + W + ")" + s});
+            const std::string k = std::to_string(n.k);
+            def(id, {dfm ? "ag::e64::mk(a.sch[" + k + "], a.scl[" + k + "])" : "(" + W + ")" + s});
         } else if (op == "lit") {
             def(id, {lit(n.lit)});
         } else if (op == "bcast") {
@@ -494,7 +530,9 @@ struct Gen {
         } else if (binary_ops().count(op)) {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string a = V(0)[size_t(c)], b = V(1)[size_t(c)];
-                if (op == "add") e.push_back(add(a, b));
+                if (op == "add" && dfm && nonneg(n.kids[0]) && nonneg(n.kids[1]))
+                    e.push_back("ag::e64::add_fast(" + a + ", " + b + ")");
+                else if (op == "add") e.push_back(add(a, b));
                 else if (op == "sub") e.push_back(sub(a, b));
                 else if (op == "mul") e.push_back(mul(a, b));
                 else if (op == "div") e.push_back(div(a, b));
@@ -782,6 +820,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     Lowering nat = low;
     nat.math = 0;
     Gen gn(P, nat, ctx, false, "n");
+    gn.direct = true;
     std::vector<std::string> nroot;
     if (emu) nroot = gn.emit(P.root);
 
@@ -794,6 +833,17 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     const std::string W = g.W, S = g.S;
     const bool sum = P.wants_sum(), store = P.wants_store();
     const bool rw = P.op == "add" || P.op == "sub";
+
+    if (emu) {
+        // The native FP64 recomputation of one sample, out of line so its
+        // registers do not weigh on the double-float fast path. It reloads its
+        // own operands at sample `s` (s < n is checked by the caller).
+        o << "__device__ __noinline__ void ag_native_lane(const AgArgs& a, ag_u64 s, double* fv) {\n";
+        if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n    const ag_u32 g = a.offset + (ag_u32)s;\n";
+        o << gn.pro.str() << gn.body.str();
+        for (int c = 0; c < P.dst_comps; ++c) o << "    fv[" << c << "] = " << nroot[size_t(c)] << ";\n";
+        o << "}\n";
+    }
 
     // The chunk body: one pass of a CTA over block*ipt*VEC consecutive samples.
     o << "template <int VEC>\n__device__ __forceinline__ void ag_chunk(const AgArgs& a, ag_u64 chunk";
@@ -835,7 +885,6 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n";
     if (emu) o << "    bool ok0_ = true;\n";
     o << g.pro.str();
-    if (emu) o << gn.pro.str();
     if (store) o << "    " << S << " out[" << P.dst_comps << "][L];\n";
     o << "#pragma unroll\n    for (int l = 0; l < L; ++l) {\n";
     if (P.has_random) o << "        const ag_u32 g = a.offset + (ag_u32)(s0[l / VEC] + (ag_u64)(l % VEC));\n";
@@ -853,8 +902,10 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     }
     if (emu) {
         // Samples outside the double-float range are recomputed natively.
-        o << "        if (!ok_) {\n" << gn.body.str();
-        for (int c = 0; c < P.dst_comps; ++c) o << "            fv" << c << " = " << nroot[size_t(c)] << ";\n";
+        o << "        const ag_u64 sl_ = s0[l / VEC] + (ag_u64)(l % VEC);\n";
+        o << "        if (!ok_ && sl_ < a.n) {\n            double nv_[" << P.dst_comps << "];\n";
+        o << "            ag_native_lane(a, sl_, nv_);\n";
+        for (int c = 0; c < P.dst_comps; ++c) o << "            fv" << c << " = nv_[" << c << "];\n";
         o << "        }\n";
     }
     for (int c = 0; c < P.dst_comps; ++c) {

@@ -1,0 +1,105 @@
+"""Autotuner: choose block shape, lane groups per thread, vector width and
+occupancy bound per plan, by timing candidate lowerings on the device.
+
+Results are cached in a JSON file keyed by the plan text, the math mode and
+the device name ($AETHER_GB300_TUNE_CACHE, else ~/.cache/aether_gb300/
+tune.json), so a plan is tuned once per device and later processes reuse the
+winner. Candidates are valid by construction (block a multiple of 32 up to
+1024, vec in {1, 2, 4}, ipt in {1, 2, 4}); a candidate that fails to compile
+or launch is skipped, never retried.
+"""
+
+import hashlib
+import json
+import os
+import threading
+
+_lock = threading.Lock()
+
+DEFAULT_CANDIDATES = [
+    dict(block=b, ipt=i, vec=v, min_blocks=m)
+    for b in (128, 256, 512)
+    for i in (1, 2)
+    for v in (0, 1)
+    for m in (0, 3, 4)
+    if not (b == 512 and m == 4)
+]
+
+
+def cache_path():
+    p = os.environ.get("AETHER_GB300_TUNE_CACHE")
+    if p:
+        return p
+    base = os.environ.get("XDG_CACHE_HOME") or os.path.join(os.path.expanduser("~"), ".cache")
+    return os.path.join(base, "aether_gb300", "tune.json")
+
+
+def _device_name():
+    import torch
+    return torch.cuda.get_device_name(torch.cuda.current_device())
+
+
+def _key(ir, math, contract):
+    h = hashlib.sha1(("%s|%d|%d|%s" % (ir, math, contract, _device_name())).encode()).hexdigest()
+    return h
+
+
+def load():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def store(key, rec):
+    with _lock:
+        data = load()
+        data[key] = rec
+        path = cache_path()
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp%d" % os.getpid()
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1)
+        os.replace(tmp, path)
+
+
+def tuned(ir, math=0, contract=-1):
+    """The cached winning lowering for a plan, or None."""
+    rec = load().get(_key(ir, math, contract))
+    return rec["lowering"] if rec else None
+
+
+def tune(make_launch, ir, math=0, contract=-1, candidates=None, reps=5, warmup=2, verbose=False):
+    """Time `make_launch(**lowering)` for each candidate lowering and cache the
+    fastest. `make_launch` returns a callable that enqueues one evaluation on
+    the current stream (aether_gb300.prepare(...)). Returns (best, results)."""
+    import torch
+    results = []
+    for cand in candidates or DEFAULT_CANDIDATES:
+        try:
+            L = make_launch(**cand)
+            for _ in range(warmup):
+                L()
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            for _ in range(reps):
+                L()
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms = ev[0].elapsed_time(ev[1]) / reps
+            info = L.plan.info()
+            results.append((ms, cand, info.registers, info.blocks_per_sm))
+            if verbose:
+                print("tune %-45s %8.4f ms  regs %3d  blocks/SM %d" % (cand, ms, info.registers, info.blocks_per_sm))
+        except Exception as e:   # candidate does not compile or launch: skip it
+            if verbose:
+                print("tune %s skipped: %s" % (cand, str(e).splitlines()[0] if str(e) else e))
+    if not results:
+        raise RuntimeError("autotune: no candidate lowering ran")
+    results.sort(key=lambda r: r[0])
+    best = results[0]
+    store(_key(ir, math, contract), {"lowering": best[1], "ms": best[0], "registers": best[2],
+                                      "blocks_per_sm": best[3], "candidates": len(results)})
+    return best[1], results

@@ -186,8 +186,8 @@ def run_ours(args):
     z = ag.Array("f64", (1,), N_FILL)
     a, b, c, d0 = (x.view() for x in arrs)
     expr = ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c)) + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0)
-    k_expr = ag.prepare(d, expr, math=math_mode)
-    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=math_mode)
+    k_expr = ag.prepare(d, expr, math=math_mode, tune=not args.no_tune)
+    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=math_mode, tune=not args.no_tune)
     torch.cuda.synchronize()
 
     def step():
@@ -290,6 +290,10 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 seed 7, generated on device)",
         "config": {"workload": WORKLOAD, "samples_expr": N_EXPR, "samples_fill": N_FILL,
                    "l2": "inputs larger than L2 (no flush)", "math": ["native FP64", "emulated FP64"][math_mode],
+                   "lowering_expr": {"block": k_expr.plan.info().block, "ipt": k_expr.plan.info().ipt,
+                                     "vec": k_expr.plan.info().vec, "registers": k_expr.plan.info().registers},
+                   "lowering_fill": {"block": k_fill.plan.info().block, "ipt": k_fill.plan.info().ipt,
+                                     "vec": k_fill.plan.info().vec, "registers": k_fill.plan.info().registers},
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
@@ -306,9 +310,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--math", type=int, default=0, help="0 native FP64, 1 emulated FP64")
+    ap.add_argument("--math", type=int, default=1, help="0 native FP64, 1 emulated FP64")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="default lowering instead of the autotuned one")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
     args = ap.parse_args()
