@@ -44,17 +44,30 @@ def _key(ir, math, contract):
     return h
 
 
-def load():
+SHIPPED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned.json")
+
+
+def load(include_shipped=True):
+    """The user's tuning cache over the winners shipped with the package
+    (tuned.json, measured on GB300 for the plans the benchmarks use)."""
+    data = {}
+    if include_shipped:
+        try:
+            with open(SHIPPED) as f:
+                data.update(json.load(f))
+        except Exception:
+            pass
     try:
         with open(cache_path()) as f:
-            return json.load(f)
+            data.update(json.load(f))
     except Exception:
-        return {}
+        pass
+    return data
 
 
 def store(key, rec):
     with _lock:
-        data = load()
+        data = load(include_shipped=False)
         data[key] = rec
         path = cache_path()
         os.makedirs(os.path.dirname(path), exist_ok=True)
