@@ -61,6 +61,7 @@ _SIGS = {
     "aether_plan_launch": (ctypes.c_int, [_P, ctypes.POINTER(AetherLaunch), _P]),
     "aether_plan_source": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_plan_release": (None, [_P]),
+    "aether_plan_launch_noalloc": (ctypes.c_int, [_P, ctypes.POINTER(AetherLaunch), _P]),
     "aether_plan_generate": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.c_char_p,
                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_nvrtc_check": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),

@@ -391,6 +391,10 @@ AG_EXPORT int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len)
     });
 }
 
+// Internal (not exported): lets other translation units of the library report
+// through aether_last_error.
+int ag_internal_fail(const char* message) { return fail(message); }
+
 AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream) {
     return guarded([&] {
         PlanObj* P = static_cast<PlanObj*>(plan);

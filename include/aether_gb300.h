@@ -128,6 +128,19 @@ int aether_plan_launch(void* plan, const AetherLaunch* args, void* stream);
 int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len);
 void aether_plan_release(void* plan);
 
+/* Launch a sum plan without allocating anything on the device. No counterpart
+ * in the reference: it exists for callers that cannot call cudaMalloc where
+ * they launch -- work being recorded into a CUDA graph, hosts that run under a
+ * fixed device-memory budget, latency-critical loops. The plan's scratch (a
+ * counter and one partial per chunk, 16 + 16 * chunks bytes) comes from a
+ * 1 MiB array compiled into the library that every GPU which loads it holds
+ * until exit; sizes that need more are refused with an error naming the
+ * limit. `args->workspace` must be NULL. The first call on a device resolves
+ * the array's address and should come before any stream capture. Calls share
+ * the array (the counter is cleared at each call), so calls whose kernels
+ * overlap on the GPU race and must be serialised by the caller. */
+int aether_plan_launch_noalloc(void* plan, const AetherLaunch* args, void* stream);
+
 /* Offline lowering, no device needed: parse and check `ir`, write the CUDA
  * source of its kernel into `buf` (up to `cap` bytes, NUL-terminated) and its
  * length into `len`. Stands in for the reference's compile-time type check of
