@@ -36,14 +36,16 @@ def _torch():
 
 def _tdtype(dtype):
     torch = _torch()
-    return {"f64": torch.float64, "f32": torch.float32}[dtype]
+    return {"f64": torch.float64, "f32": torch.float32, "ff": torch.float32}[dtype]
 
 
 class Array:
     """Owning SoA array on the GPU: `shape` components x `n` samples.
 
-    `data` is a torch tensor (components, capacity); plane c starts at
-    c * capacity elements, 256-byte aligned for both f64 and f32."""
+    `data` is a torch tensor (planes, capacity); plane c starts at
+    c * capacity elements, 256-byte aligned for both f64 and f32. An "ff"
+    array (the precision form's float-float storage) holds the hi planes of
+    its components followed by their lo planes."""
 
     def __init__(self, dtype, shape, n, device="cuda", data=None):
         if isinstance(shape, int):
@@ -53,13 +55,21 @@ class Array:
         self.comps = 1
         for s in self.shape:
             self.comps *= s
+        self.planes = self.comps * (2 if dtype == "ff" else 1)
         self.n = int(n)
         if data is not None:
             self.data = data
             self.capacity = data.shape[1]
         else:
             self.capacity = quantized_capacity(n)
-            self.data = _torch().zeros((self.comps, self.capacity), dtype=_tdtype(dtype), device=device)
+            self.data = _torch().zeros((self.planes, self.capacity), dtype=_tdtype(dtype), device=device)
+
+    def host_ff(self):
+        """An ff array's values, hi + lo, as float64 (comps, n)."""
+        import numpy as np
+        h = self.data[: self.comps, : self.n].cpu().numpy().astype(np.float64)
+        lo = self.data[self.comps:, : self.n].cpu().numpy().astype(np.float64)
+        return h + lo
 
     @classmethod
     def wrap(cls, tensor, shape=None, n=None):

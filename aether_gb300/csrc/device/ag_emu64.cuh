@@ -330,14 +330,32 @@ __device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
     return (qq & 2) ? neg(v) : v;
 }
 // Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.
+__device__ __forceinline__ df dfc(double x);
+
+// Arguments up to 2^19 pi/2 reduce in FP64 instead (three-part pi/2 with
+// 33-bit leading parts, exact products): the one place the double-float
+// lowering uses the FP64 pipe beyond the final reassembly. Larger arguments
+// take the native path, whose FP64 reduction is total.
 __device__ __forceinline__ df trig_(df x, bool want_cos, bool& ok) {
-    ok = ok && fabsf(x.hi) < 6000.0f;
-    const float kf = rint_f(__fmul_rn(x.hi, AG_TWO_OVER_PI));
-    const float r1 = __fmaf_rn(-kf, AG_PIO2_1, x.hi);
-    df r = two_sum(r1, x.lo);
-    r = sub(r, two_prod(kf, AG_PIO2_2));
-    r = add(r, __fmul_rn(-kf, AG_PIO2_3));
-    return trig_core(r, rint_i(__fmul_rn(x.hi, AG_TWO_OVER_PI)), want_cos);
+    const float ax = fabsf(x.hi);
+    ok = ok && ax < 823549.0f;
+    df r;
+    int q;
+    if (ax < 6000.0f) {
+        const float kf = rint_f(__fmul_rn(x.hi, AG_TWO_OVER_PI));
+        const float r1 = __fmaf_rn(-kf, AG_PIO2_1, x.hi);
+        r = two_sum(r1, x.lo);
+        r = sub(r, two_prod(kf, AG_PIO2_2));
+        r = add(r, __fmul_rn(-kf, AG_PIO2_3));
+        q = rint_i(__fmul_rn(x.hi, AG_TWO_OVER_PI));
+    } else {
+        const double xd = (double)x.hi + (double)x.lo;
+        const double kd = rint(xd * 0.63661977236758134);
+        const double rd = ((xd - kd * AG_PIO2_D1) - kd * AG_PIO2_D2) - kd * AG_PIO2_D3;
+        r = dfc(rd);
+        q = (int)kd;
+    }
+    return trig_core(r, q, want_cos);
 }
 __device__ __forceinline__ df sin_(df x, bool& ok) { return trig_(x, false, ok); }
 __device__ __forceinline__ df cos_(df x, bool& ok) { return trig_(x, true, ok); }

@@ -122,6 +122,18 @@ def main():
     out.append("#define AG_PIO2_2 %s" % fl(p2))
     out.append("#define AG_PIO2_3 %s" % fl(p3))
     out.append("#define AG_TWO_OVER_PI %s" % fl(2 / mp.pi))
+    # pi/2 as three doubles for the FP64 reduction of large arguments: the
+    # first two with 33 significant bits so k*P for |k| < 2^19 is exact.
+    def trunc_d(v, bits):
+        v = mp.mpf(v)
+        e = mp.floor(mp.log(abs(v), 2))
+        scale = mp.mpf(2) ** (bits - 1 - e)
+        return mp.floor(abs(v) * scale) / scale * mp.sign(v)
+    d1 = trunc_d(pio2, 33)
+    d2 = trunc_d(pio2 - d1, 33)
+    d3 = mp.mpf(float(pio2 - d1 - d2))
+    for name, v in (("AG_PIO2_D1", d1), ("AG_PIO2_D2", d2), ("AG_PIO2_D3", d3)):
+        out.append("#define %s %s" % (name, float(v).hex()))
     pih, pil = split2(mp.pi)
     out.append("#define AG_PI_HI %s" % fl(pih))
     out.append("#define AG_PI_LO %s" % fl(pil))

@@ -420,10 +420,22 @@ struct Gen {
         return r;
     }
 
-    Gen(const Plan& p, const Lowering& l, const std::vector<int>& c, bool df_mode = false, std::string prefix = "t")
+    Gen(const Plan& p, const Lowering& l, const std::vector<int>& c, bool df_mode = false, std::string prefix = "t",
+        bool force_double = false)
         : P(p), L(l), ctx(c), val(p.nodes.size()), done(p.nodes.size(), 0), dfm(df_mode), pre(std::move(prefix)) {
-        W = dfm ? "ag::e64::df" : (P.dst_dtype == DType::F64 ? "double" : "float");
+        W = dfm ? "ag::e64::df" : ((P.dst_dtype == DType::F64 || force_double) ? "double" : "float");
         S = P.dst_dtype == DType::F64 ? "double" : "float";
+    }
+
+    // A double-float value that is an exact float (an f32 operand): products
+    // of two of them are exact two-products, no double-float multiply.
+    bool exact_f32(int id) const {
+        const Node& n = P.nodes[size_t(id)];
+        return dfm && n.op == "in" && n.dtype == DType::F32;
+    }
+    std::string mulx(int ia, int ib, const std::string& a, const std::string& b) const {
+        if (exact_f32(ia) && exact_f32(ib)) return "ag::e64::two_prod(" + a + ".hi, " + b + ".hi)";
+        return mul(a, b);
     }
 
     std::string add(const std::string& a, const std::string& b) const {
@@ -498,6 +510,8 @@ struct Gen {
                           std::to_string(c) + " * a.pitch[" + std::to_string(n.k) + "] + " + (c0 ? "0" : "s") + "]";
                 if (pbool) {
                     e.push_back("(" + src + " != 0)");
+                } else if (dfm && n.dtype == DType::F32) {
+                    e.push_back("ag::e64::mk((float)" + src + ", 0.0f)");   // exact
                 } else if (dfm) {
                     out_for(id) << "        " << okv(id) << " = " << okv(id) << " && ag::e64::in_range((double)" << src << ");\n";
                     e.push_back("ag::e64::from_double((double)" + src + ")");
@@ -534,7 +548,7 @@ struct Gen {
                     e.push_back("ag::e64::add_fast(" + a + ", " + b + ")");
                 else if (op == "add") e.push_back(add(a, b));
                 else if (op == "sub") e.push_back(sub(a, b));
-                else if (op == "mul") e.push_back(mul(a, b));
+                else if (op == "mul") e.push_back(mulx(n.kids[0], n.kids[1], a, b));
                 else if (op == "div") e.push_back(div(a, b));
                 else e.push_back(call(op, {a, b}, id));
             }
@@ -702,7 +716,7 @@ struct Gen {
             const auto& a = V(0);
             const int m = K(0).comps;
             auto term = [&](int c) -> std::string {
-                if (op == "dot") return mul(a[size_t(c)], V(1)[size_t(c)]);
+                if (op == "dot") return mulx(n.kids[0], n.kids[1], a[size_t(c)], V(1)[size_t(c)]);
                 if (op == "sum") return a[size_t(c)];
                 if (op == "maxnorm") return call("abs", {a[size_t(c)]}, id);
                 return mul(a[size_t(c)], a[size_t(c)]);
@@ -812,14 +826,18 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         // A node used both inside and outside at0 would need two copies; the
         // parser keys its memo by context, so such nodes are already distinct.
     }
-    // Emulated FP64: the tree is generated twice, once in double-float (the
-    // fast path) and once on the native FP64 pipe (the per-lane fallback).
-    const bool emu = low.math == 1 && P.dst_dtype == DType::F64;
+    // Emulated FP64 (math 1, f64 plans) and the precision form (math 2, f32
+    // and ff plans): the tree is generated in double-float (the fast path) and
+    // once more on the native FP64 pipe (the per-lane fallback).
+    const bool emu = (low.math == 1 && P.dst_dtype == DType::F64) || (low.math == 2 && P.dst_dtype != DType::F64);
+    const bool prec = emu && P.dst_dtype != DType::F64;   // float storage, float-float working values
+    const bool dst_ff = P.dst_dtype == DType::FF;
+    if (dst_ff && !prec) fail("ff destinations are written by the precision form (math = 2)");
     Gen g(P, low, ctx, emu, emu ? "d" : "t");
     const std::vector<std::string> root = g.emit(P.root);
     Lowering nat = low;
     nat.math = 0;
-    Gen gn(P, nat, ctx, false, "n");
+    Gen gn(P, nat, ctx, false, "n", true);
     gn.direct = true;
     std::vector<std::string> nroot;
     if (emu) nroot = gn.emit(P.root);
@@ -828,11 +846,13 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     std::ostringstream o;
     o << "// generated by aether_gb300 from an aether-ir/1 plan\n";
     o << "#include \"ag_device.cuh\"\n";
-    if (low.math == 1) o << "#include \"ag_emu64.cuh\"\n";
+    if (low.math >= 1) o << "#include \"ag_emu64.cuh\"\n";
     o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
     const std::string W = g.W, S = g.S;
+    const int OC = P.dst_comps * (dst_ff ? 2 : 1);   // stored planes (ff: hi planes, then lo planes)
     const bool sum = P.wants_sum(), store = P.wants_store();
     const bool rw = P.op == "add" || P.op == "sub";
+    if (rw && prec) fail("+= and -= are lowered by the native and emulated-FP64 forms, not the precision form");
 
     if (emu) {
         // The native FP64 recomputation of one sample, out of line so its
@@ -847,7 +867,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
 
     // The chunk body: one pass of a CTA over block*ipt*VEC consecutive samples.
     o << "template <int VEC>\n__device__ __forceinline__ void ag_chunk(const AgArgs& a, ag_u64 chunk";
-    if (sum) o << ", double& acc_h, double& acc_c";
+    if (sum) o << (prec ? ", ag::e64::df& acc" : ", double& acc_h, double& acc_c");
     o << ") {\n";
     o << "    constexpr int L = AG_IPT * VEC;\n";
     o << "    ag_u64 s0[AG_IPT];\n";
@@ -885,7 +905,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n";
     if (emu) o << "    bool ok0_ = true;\n";
     o << g.pro.str();
-    if (store) o << "    " << S << " out[" << P.dst_comps << "][L];\n";
+    if (store) o << "    " << S << " out[" << OC << "][L];\n";
     o << "#pragma unroll\n    for (int l = 0; l < L; ++l) {\n";
     if (P.has_random) o << "        const ag_u32 g = a.offset + (ag_u32)(s0[l / VEC] + (ag_u64)(l % VEC));\n";
     if (emu) o << "        bool ok_ = ok0_;\n";
@@ -893,7 +913,10 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     // Final working values of the output components.
     const std::string FW = emu ? "double" : W;
     for (int c = 0; c < P.dst_comps; ++c) {
-        if (emu) {
+        if (prec) {
+            o << "        ag::e64::df fv" << c << " = " << root[size_t(c)] << ";\n";
+            o << "        ok_ = ok_ && ag::e64::out_ok(fv" << c << ");\n";
+        } else if (emu) {
             o << "        double fv" << c << " = ag::e64::to_double(" << root[size_t(c)] << ");\n";
             o << "        ok_ = ok_ && ag::e64::out_ok(" << root[size_t(c)] << ");\n";
         } else {
@@ -905,24 +928,38 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         o << "        const ag_u64 sl_ = s0[l / VEC] + (ag_u64)(l % VEC);\n";
         o << "        if (!ok_ && sl_ < a.n) {\n            double nv_[" << P.dst_comps << "];\n";
         o << "            ag_native_lane(a, sl_, nv_);\n";
-        for (int c = 0; c < P.dst_comps; ++c) o << "            fv" << c << " = nv_[" << c << "];\n";
+        for (int c = 0; c < P.dst_comps; ++c)
+            o << "            fv" << c << " = " << (prec ? "ag::e64::dfc(nv_[" + std::to_string(c) + "])" : "nv_[" + std::to_string(c) + "]") << ";\n";
         o << "        }\n";
     }
     for (int c = 0; c < P.dst_comps; ++c) {
         const std::string v = "fv" + std::to_string(c);
-        if (store) {
-            if (P.op == "set" || P.op == "setsum") o << "        out[" << c << "][l] = (" << S << ")" << v << ";\n";
-            else if (P.op == "add") o << "        out[" << c << "][l] = (" << S << ")ag::rn_add((" << FW << ")cur[" << c << "][l], " << v << ");\n";
-            else o << "        out[" << c << "][l] = (" << S << ")ag::rn_sub((" << FW << ")cur[" << c << "][l], " << v << ");\n";
+        if (!store) continue;
+        if (prec) {
+            // float-float value: rounded once to float, or stored as its (hi, lo) planes
+            if (dst_ff) {
+                o << "        out[" << c << "][l] = " << v << ".hi;\n";
+                o << "        out[" << (P.dst_comps + c) << "][l] = " << v << ".lo;\n";
+            } else {
+                o << "        out[" << c << "][l] = __fadd_rn(" << v << ".hi, " << v << ".lo);\n";
+            }
+        } else if (P.op == "set" || P.op == "setsum") {
+            o << "        out[" << c << "][l] = (" << S << ")" << v << ";\n";
+        } else if (P.op == "add") {
+            o << "        out[" << c << "][l] = (" << S << ")ag::rn_add((" << FW << ")cur[" << c << "][l], " << v << ");\n";
+        } else {
+            o << "        out[" << c << "][l] = (" << S << ")ag::rn_sub((" << FW << ")cur[" << c << "][l], " << v << ");\n";
         }
     }
     if (sum) {
-        o << "        if (s0[l / VEC] + (ag_u64)(l % VEC) < a.n) ag::neumaier_add(acc_h, acc_c, (double)fv0);\n";
+        o << "        if (s0[l / VEC] + (ag_u64)(l % VEC) < a.n) ";
+        if (prec) o << "acc = ag::e64::add(acc, fv0);\n";   // per-thread float-float sum
+        else o << "ag::neumaier_add(acc_h, acc_c, (double)fv0);\n";
     }
     o << "    }\n";
     if (store) {
         o << "    " << S << "* __restrict__ po = (" << S << "*)a.dst;\n";
-        o << "#pragma unroll\n    for (int c = 0; c < " << P.dst_comps << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, " << S
+        o << "#pragma unroll\n    for (int c = 0; c < " << OC << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, " << S
           << ">::store(po + c * a.dst_pitch, s0[j], a.n, &out[c][j * VEC]);\n";
     }
     o << "}\n";
@@ -938,7 +975,12 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         k << "    const ag_u64 per = (ag_u64)AG_BLOCK * AG_IPT * " << V << ";\n";
         k << "    const ag_u64 nchunks = (a.n + per - 1) / per;\n";
         k << "    for (ag_u64 ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {\n";
-        if (sum) {
+        if (sum && prec) {
+            // float-float per thread, FP64 from the warp tree on
+            k << "        ag::e64::df acc = ag::e64::mk(0.0f, 0.0f);\n";
+            k << "        ag_chunk<" << V << ">(a, ch, acc);\n";
+            k << "        ag::sum_chunk_finish<AG_BLOCK>(a, ch, nchunks, ag::e64::f2d(acc.hi), ag::e64::f2d(acc.lo));\n";
+        } else if (sum) {
             k << "        double h = 0.0, c = 0.0;\n";
             k << "        ag_chunk<" << V << ">(a, ch, h, c);\n";
             k << "        ag::sum_chunk_finish<AG_BLOCK>(a, ch, nchunks, h, c);\n";
