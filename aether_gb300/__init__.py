@@ -245,7 +245,71 @@ def global_sum(expr, n, dtype="f64", stream=None, workspace=None, **kw):
     return out
 
 
+def _stream(stream):
+    return ctypes.c_void_p(stream if stream is not None else _torch().cuda.current_stream().cuda_stream)
+
+
+class Batch:
+    """Many assignments in one persistent launch (aether_batch_*).
+
+    `launches` is a list of Launch objects (from prepare()); their plans are
+    grouped, one kernel is generated for the distinct plans, and the work list
+    holds one argument block per launch."""
+
+    def __init__(self, launches, block=0, ipt=0):
+        plans, index = [], {}
+        for L in launches:
+            h = L.plan.handle.value
+            if h not in index:
+                index[h] = len(plans)
+                plans.append(L.plan)
+        self._plans = plans
+        self._launches = list(launches)
+        arr = (ctypes.c_void_p * len(plans))(*[p.handle for p in plans])
+        h = ctypes.c_void_p()
+        low = lowering(block, ipt)
+        _abi.check(_abi.lib().aether_batch_create(arr, len(plans), ctypes.byref(low), ctypes.byref(h)))
+        self.handle = h
+        items = (_abi.AetherBatchItem * max(1, len(launches)))()
+        for i, L in enumerate(launches):
+            items[i].plan = index[L.plan.handle.value]
+            items[i].args = L.args
+        self._items = items
+        _abi.check(_abi.lib().aether_batch_set_items(self.handle, items, len(launches), _stream(None)))
+
+    def launch(self, stream=None):
+        _abi.check(_abi.lib().aether_batch_launch(self.handle, _stream(stream)))
+
+    def capture(self, stream):
+        """Capture one launch into a CUDA graph on `stream` (a non-default
+        stream handle, e.g. torch.cuda.Stream().cuda_stream)."""
+        _abi.check(_abi.lib().aether_batch_capture(self.handle, ctypes.c_void_p(stream)))
+
+    def replay(self, stream=None):
+        _abi.check(_abi.lib().aether_batch_replay(self.handle, _stream(stream)))
+
+    def info(self):
+        i = _abi.AetherBatchInfo()
+        _abi.check(_abi.lib().aether_batch_info(self.handle, ctypes.byref(i)))
+        return i
+
+    def launch_each(self, stream=None):
+        """The per-call baseline: one plain launch per item from a C loop."""
+        n = len(self._launches)
+        plans = (ctypes.c_void_p * n)(*[L.plan.handle for L in self._launches])
+        args = (_abi.AetherLaunch * n)(*[L.args for L in self._launches])
+        _abi.check(_abi.lib().aether_plan_launch_many(plans, args, n, _stream(stream)))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _abi.lib().aether_batch_release(self.handle)
+        except Exception:
+            pass
+
+
 __all__ = [
+    "Batch",
     "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
     "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
     "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",

@@ -40,6 +40,16 @@ class AetherPlanInfo(ctypes.Structure):
                 ("registers", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("compile_ms", ctypes.c_double)]
 
 
+class AetherBatchItem(ctypes.Structure):
+    _fields_ = [("plan", ctypes.c_int), ("reserved", ctypes.c_int), ("args", AetherLaunch)]
+
+
+class AetherBatchInfo(ctypes.Structure):
+    _fields_ = [("hash", ctypes.c_uint64), ("n_plans", ctypes.c_int), ("n_items", ctypes.c_int),
+                ("total_tiles", ctypes.c_uint64), ("block", ctypes.c_int), ("ipt", ctypes.c_int),
+                ("registers", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("compile_ms", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); every symbol include/aether_gb300.h declares.
 _P = ctypes.c_void_p
 _SIGS = {
@@ -62,6 +72,15 @@ _SIGS = {
     "aether_plan_source": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_plan_release": (None, [_P]),
     "aether_plan_launch_noalloc": (ctypes.c_int, [_P, ctypes.POINTER(AetherLaunch), _P]),
+    "aether_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(AetherLowering),
+                                           ctypes.POINTER(_P)]),
+    "aether_batch_set_items": (ctypes.c_int, [_P, ctypes.POINTER(AetherBatchItem), ctypes.c_int, _P]),
+    "aether_batch_launch": (ctypes.c_int, [_P, _P]),
+    "aether_batch_capture": (ctypes.c_int, [_P, _P]),
+    "aether_batch_replay": (ctypes.c_int, [_P, _P]),
+    "aether_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(AetherBatchInfo)]),
+    "aether_batch_release": (None, [_P]),
+    "aether_plan_launch_many": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(AetherLaunch), ctypes.c_int, _P]),
     "aether_plan_generate": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.c_char_p,
                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_nvrtc_check": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),

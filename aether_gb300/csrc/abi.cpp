@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -400,52 +401,60 @@ AG_EXPORT int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len)
 // through aether_last_error.
 int ag_internal_fail(const char* message) { return fail(message); }
 
+// Validate a launch against its plan and build the kernel's argument block.
+// Returns whether every plane is 16-byte aligned (the vectorized kernel).
+static bool make_args(const PlanObj* P, const AetherLaunch* a, AgArgsHost& k) {
+    const ag::Plan& pl = P->plan;
+    if (a->n > 0xFFFFFFFFull) throw std::runtime_error("plan_launch: n exceeds the 32-bit sample index");
+    if (uint64_t(a->sample_offset) + a->n - 1 > 0xFFFFFFFFull)
+        throw std::runtime_error("plan_launch: sample_offset + n exceeds the 32-bit sample index");
+    if (int(a->n_operands) < pl.n_operands)
+        throw std::runtime_error("plan_launch: plan reads " + std::to_string(pl.n_operands) + " operands, " +
+                                 std::to_string(a->n_operands) + " given");
+    if (int(a->n_scalars) < pl.n_scalars) throw std::runtime_error("plan_launch: too few scalars");
+    if (int(a->n_keys) < pl.n_keys) throw std::runtime_error("plan_launch: too few generator keys");
+    k = AgArgsHost{};
+    k.n = a->n;
+    k.offset = a->sample_offset;
+    bool aligned = true;
+    if (pl.wants_store()) {
+        if (!a->dst) throw std::runtime_error("plan_launch: null destination");
+        if (pl.dst_comps > 1 && a->dst_pitch < a->n) throw std::runtime_error("plan_launch: destination pitch smaller than n");
+        k.dst = static_cast<char*>(a->dst);
+        k.dst_pitch = a->dst_pitch ? a->dst_pitch : a->n;
+        const int es = ag::dtype_size(pl.dst_dtype);
+        aligned = aligned && (reinterpret_cast<uintptr_t>(a->dst) % 16 == 0) &&
+                  (pl.dst_comps == 1 || (k.dst_pitch * es) % 16 == 0);
+    }
+    for (int i = 0; i < pl.n_operands; ++i) {
+        const AetherOperand& o = a->operands[i];
+        if (!o.ptr) throw std::runtime_error("plan_launch: operand " + std::to_string(i) + " is null");
+        const int comps = pl.operand_comps[size_t(i)];
+        const uint64_t pitch = o.pitch ? o.pitch : a->n;
+        if (comps > 1 && pitch < a->n)
+            throw std::runtime_error("plan_launch: operand " + std::to_string(i) + " pitch smaller than n");
+        k.ops[i] = static_cast<const char*>(o.ptr);
+        k.pitch[i] = pitch;
+        const int es = ag::dtype_size(pl.operand_dtype[size_t(i)]);
+        aligned = aligned && (reinterpret_cast<uintptr_t>(o.ptr) % 16 == 0) && (comps == 1 || (pitch * es) % 16 == 0);
+    }
+    for (int i = 0; i < pl.n_scalars; ++i) {
+        k.sc[i] = a->scalars[i];
+        k.sch[i] = float(a->scalars[i]);
+        k.scl[i] = std::isfinite(k.sch[i]) ? float(a->scalars[i] - double(k.sch[i])) : 0.0f;
+    }
+    for (int i = 0; i < pl.n_keys; ++i) k.key[i] = a->keys[i];
+    return aligned;
+}
+
 AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream) {
     return guarded([&] {
         PlanObj* P = static_cast<PlanObj*>(plan);
         if (!P || !a) throw std::runtime_error("plan_launch: null argument");
         const ag::Plan& pl = P->plan;
         if (a->n == 0) return;
-        if (a->n > 0xFFFFFFFFull) throw std::runtime_error("plan_launch: n exceeds the 32-bit sample index");
-        if (uint64_t(a->sample_offset) + a->n - 1 > 0xFFFFFFFFull)
-            throw std::runtime_error("plan_launch: sample_offset + n exceeds the 32-bit sample index");
-        if (int(a->n_operands) < pl.n_operands)
-            throw std::runtime_error("plan_launch: plan reads " + std::to_string(pl.n_operands) + " operands, " +
-                                     std::to_string(a->n_operands) + " given");
-        if (int(a->n_scalars) < pl.n_scalars) throw std::runtime_error("plan_launch: too few scalars");
-        if (int(a->n_keys) < pl.n_keys) throw std::runtime_error("plan_launch: too few generator keys");
-        AgArgsHost k{};
-        k.n = a->n;
-        k.offset = a->sample_offset;
-        bool aligned = true;
-        if (pl.wants_store()) {
-            if (!a->dst) throw std::runtime_error("plan_launch: null destination");
-            if (pl.dst_comps > 1 && a->dst_pitch < a->n)
-                throw std::runtime_error("plan_launch: destination pitch smaller than n");
-            k.dst = static_cast<char*>(a->dst);
-            k.dst_pitch = a->dst_pitch ? a->dst_pitch : a->n;
-            const int es = ag::dtype_size(pl.dst_dtype);
-            aligned = aligned && (reinterpret_cast<uintptr_t>(a->dst) % 16 == 0) &&
-                      (pl.dst_comps == 1 || (k.dst_pitch * es) % 16 == 0);
-        }
-        for (int i = 0; i < pl.n_operands; ++i) {
-            const AetherOperand& o = a->operands[i];
-            if (!o.ptr) throw std::runtime_error("plan_launch: operand " + std::to_string(i) + " is null");
-            const int comps = pl.operand_comps[size_t(i)];
-            const uint64_t pitch = o.pitch ? o.pitch : a->n;
-            if (comps > 1 && pitch < a->n)
-                throw std::runtime_error("plan_launch: operand " + std::to_string(i) + " pitch smaller than n");
-            k.ops[i] = static_cast<const char*>(o.ptr);
-            k.pitch[i] = pitch;
-            const int es = ag::dtype_size(pl.operand_dtype[size_t(i)]);
-            aligned = aligned && (reinterpret_cast<uintptr_t>(o.ptr) % 16 == 0) && (comps == 1 || (pitch * es) % 16 == 0);
-        }
-        for (int i = 0; i < pl.n_scalars; ++i) {
-            k.sc[i] = a->scalars[i];
-            k.sch[i] = float(a->scalars[i]);
-            k.scl[i] = std::isfinite(k.sch[i]) ? float(a->scalars[i] - double(k.sch[i])) : 0.0f;
-        }
-        for (int i = 0; i < pl.n_keys; ++i) k.key[i] = a->keys[i];
+        AgArgsHost k;
+        const bool aligned = make_args(P, a, k);
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         const bool vect = aligned && P->vec > 1;
         if (pl.wants_sum()) {
@@ -482,6 +491,224 @@ AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream
                             params, 0, s),
            "cudaLaunchKernel");
     });
+}
+
+// ============================================================================
+// Batches: many plan launches as one persistent kernel over a device work list
+// ============================================================================
+namespace {
+
+struct AgItemHost {
+    AgArgsHost a;
+    uint64_t tile0;
+    int plan;
+    int pad;
+};
+static_assert(sizeof(AgItemHost) == 648, "AgItem layout");
+
+struct BatchObj {
+    std::vector<PlanObj*> plans;
+    std::vector<int> vecs;
+    int block = 256, ipt = 1;
+    std::string name, source;
+    ag::Compiled compiled;
+    cudaLibrary_t library = nullptr;
+    cudaKernel_t kernel = nullptr;
+    int blocks_per_sm = 1, sms = 1, registers = 0;
+    AgItemHost* host_items = nullptr;   // pinned staging of the work list
+    void* dev_items = nullptr;
+    size_t cap_items = 0;
+    int n_items = 0;
+    uint64_t total_tiles = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t graph_tiles = 0;
+    int graph_items = 0;
+};
+
+void batch_enqueue(BatchObj* B, cudaStream_t s) {
+    if (B->total_tiles == 0) return;
+    const uint64_t cap = uint64_t(std::max(B->blocks_per_sm, 1)) * uint64_t(B->sms);
+    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min(B->total_tiles, cap)));
+    void* items = B->dev_items;
+    int n = B->n_items;
+    uint64_t tiles = B->total_tiles;
+    void* params[] = {&items, &n, &tiles};
+    ck(cudaLaunchKernel(reinterpret_cast<const void*>(B->kernel), dim3(grid), dim3(unsigned(B->block)), params, 0, s),
+       "cudaLaunchKernel(batch)");
+}
+
+}  // namespace
+
+AG_EXPORT int aether_batch_create(void* const* plans, int n_plans, const AetherLowering* lowering, void** out) {
+    return guarded([&] {
+        if (!plans || n_plans <= 0 || !out) throw std::runtime_error("batch_create: no plans");
+        auto B = std::make_unique<BatchObj>();
+        if (lowering && lowering->block > 0) B->block = lowering->block;
+        if (lowering && lowering->ipt > 0) B->ipt = lowering->ipt;
+        if (B->block % 32 || B->block < 32 || B->block > 1024)
+            throw std::runtime_error("batch_create: block must be a multiple of 32 in [32, 1024]");
+        if (B->ipt < 1 || B->ipt > 8) throw std::runtime_error("batch_create: ipt must be in [1, 8]");
+        std::vector<const ag::Plan*> ps;
+        std::vector<ag::Lowering> lows;
+        std::string key = std::to_string(B->block) + "/" + std::to_string(B->ipt);
+        for (int p = 0; p < n_plans; ++p) {
+            PlanObj* P = static_cast<PlanObj*>(plans[p]);
+            if (!P) throw std::runtime_error("batch_create: null plan");
+            if (P->plan.wants_sum()) throw std::runtime_error("batch_create: sum plans cannot join a batch");
+            B->plans.push_back(P);
+            ps.push_back(&P->plan);
+            ag::Lowering l = P->low;
+            l.block = B->block;
+            l.ipt = B->ipt;
+            lows.push_back(l);
+            B->vecs.push_back(ag::effective_vec(P->plan, l));
+            key += "|" + P->name + "/" + std::to_string(l.math) + "/" + std::to_string(l.contract);
+        }
+        char nm[40];
+        std::snprintf(nm, sizeof nm, "ag_batch_%08x", unsigned(ag::fnv1a(key) & 0xffffffffu));
+        B->name = nm;
+        B->source = ag::generate_batch_source(ps, lows, B->block, B->ipt, B->name);
+        ck(cudaFree(nullptr), "CUDA context");
+        B->compiled = ag::compile_cached(B->source, "batch");
+        ck(cudaLibraryLoadData(&B->library, B->compiled.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+           "cudaLibraryLoadData(batch)");
+        ck(cudaLibraryGetKernel(&B->kernel, B->library, B->name.c_str()), "cudaLibraryGetKernel(batch)");
+        cudaFuncAttributes fa{};
+        ck(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(B->kernel)), "cudaFuncGetAttributes");
+        B->registers = fa.numRegs;
+        ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&B->blocks_per_sm, reinterpret_cast<const void*>(B->kernel),
+                                                         B->block, 0), "occupancy");
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&B->sms, cudaDevAttrMultiProcessorCount, dev);
+        *out = B.release();
+    });
+}
+
+AG_EXPORT int aether_batch_set_items(void* batch, const AetherBatchItem* items, int n_items, void* stream) {
+    return guarded([&] {
+        BatchObj* B = static_cast<BatchObj*>(batch);
+        if (!B || (!items && n_items)) throw std::runtime_error("batch_set_items: null argument");
+        if (n_items < 0) throw std::runtime_error("batch_set_items: negative item count");
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (size_t(n_items) > B->cap_items) {
+            size_t cap = std::max<size_t>(size_t(n_items), B->cap_items * 2);
+            if (B->host_items) cudaFreeHost(B->host_items);
+            if (B->dev_items) cudaFree(B->dev_items);
+            B->host_items = nullptr;
+            B->dev_items = nullptr;
+            B->cap_items = 0;
+            void* h = nullptr;
+            ck(cudaMallocHost(&h, cap * sizeof(AgItemHost)), "cudaMallocHost(work list)");
+            B->host_items = static_cast<AgItemHost*>(h);
+            ck(cudaMalloc(&B->dev_items, cap * sizeof(AgItemHost)), "cudaMalloc(work list)");
+            B->cap_items = cap;
+        }
+        uint64_t tiles = 0;
+        for (int i = 0; i < n_items; ++i) {
+            const AetherBatchItem& it = items[i];
+            if (it.plan < 0 || size_t(it.plan) >= B->plans.size())
+                throw std::runtime_error("batch_set_items: item " + std::to_string(i) + " names plan " +
+                                         std::to_string(it.plan) + " of " + std::to_string(B->plans.size()));
+            AgItemHost& h = B->host_items[i];
+            h = AgItemHost{};
+            if (it.args.n > 0 && !make_args(B->plans[size_t(it.plan)], &it.args, h.a))
+                throw std::runtime_error("batch_set_items: item " + std::to_string(i) +
+                                         " has a plane that is not 16-byte aligned");
+            h.tile0 = tiles;
+            h.plan = it.plan;
+            const uint64_t per = uint64_t(B->block) * uint64_t(B->ipt) * uint64_t(B->vecs[size_t(it.plan)]);
+            tiles += (it.args.n + per - 1) / per;
+        }
+        B->n_items = n_items;
+        B->total_tiles = tiles;
+        if (n_items) {
+            ck(cudaMemcpyAsync(B->dev_items, B->host_items, size_t(n_items) * sizeof(AgItemHost),
+                               cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(work list)");
+            ck(cudaStreamSynchronize(s), "cudaStreamSynchronize(work list)");   // the staging buffer is reused
+        }
+    });
+}
+
+AG_EXPORT int aether_batch_launch(void* batch, void* stream) {
+    return guarded([&] {
+        BatchObj* B = static_cast<BatchObj*>(batch);
+        if (!B) throw std::runtime_error("batch_launch: null batch");
+        batch_enqueue(B, static_cast<cudaStream_t>(stream));
+    });
+}
+
+AG_EXPORT int aether_batch_capture(void* batch, void* stream) {
+    return guarded([&] {
+        BatchObj* B = static_cast<BatchObj*>(batch);
+        if (!B) throw std::runtime_error("batch_capture: null batch");
+        if (!stream) throw std::runtime_error("batch_capture: capture needs a non-default stream");
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (B->exec) cudaGraphExecDestroy(B->exec);
+        if (B->graph) cudaGraphDestroy(B->graph);
+        B->exec = nullptr;
+        B->graph = nullptr;
+        ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        try {
+            batch_enqueue(B, s);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        ck(cudaStreamEndCapture(s, &B->graph), "cudaStreamEndCapture");
+        ck(cudaGraphInstantiate(&B->exec, B->graph, 0), "cudaGraphInstantiate");
+        B->graph_tiles = B->total_tiles;
+        B->graph_items = B->n_items;
+    });
+}
+
+AG_EXPORT int aether_batch_replay(void* batch, void* stream) {
+    return guarded([&] {
+        BatchObj* B = static_cast<BatchObj*>(batch);
+        if (!B || !B->exec) throw std::runtime_error("batch_replay: nothing captured");
+        if (B->graph_tiles != B->total_tiles || B->graph_items != B->n_items)
+            throw std::runtime_error("batch_replay: the work list changed its tiling since the capture; capture again");
+        ck(cudaGraphLaunch(B->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch");
+    });
+}
+
+AG_EXPORT int aether_batch_info(void* batch, AetherBatchInfo* info) {
+    return guarded([&] {
+        const BatchObj* B = static_cast<const BatchObj*>(batch);
+        if (!B || !info) throw std::runtime_error("batch_info: null argument");
+        info->hash = B->compiled.hash;
+        info->n_plans = int(B->plans.size());
+        info->n_items = B->n_items;
+        info->total_tiles = B->total_tiles;
+        info->block = B->block;
+        info->ipt = B->ipt;
+        info->registers = B->registers;
+        info->blocks_per_sm = B->blocks_per_sm;
+        info->compile_ms = B->compiled.compile_ms;
+    });
+}
+
+AG_EXPORT void aether_batch_release(void* batch) {
+    BatchObj* B = static_cast<BatchObj*>(batch);
+    if (!B) return;
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    if (B->host_items) cudaFreeHost(B->host_items);
+    if (B->dev_items) cudaFree(B->dev_items);
+    if (B->library) cudaLibraryUnload(B->library);
+    delete B;
+}
+
+AG_EXPORT int aether_plan_launch_many(void* const* plans, const AetherLaunch* args, int count, void* stream) {
+    if (count < 0 || (count && (!plans || !args))) return fail("plan_launch_many: bad arguments");
+    for (int i = 0; i < count; ++i) {
+        const int rc = aether_plan_launch(plans[i], &args[i], stream);
+        if (rc != AETHER_OK) return rc;
+    }
+    return AETHER_OK;
 }
 
 AG_EXPORT int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* buf, size_t cap,

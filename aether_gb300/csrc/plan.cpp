@@ -806,7 +806,8 @@ std::string kernel_base(const Plan& plan, const std::string& text) {
     return buf;
 }
 
-std::string generate_source(const Plan& plan_in, const Lowering& low, const std::string& base) {
+std::string generate_source(const Plan& plan_in, const Lowering& low, const std::string& base,
+                            const std::string& suffix, bool chunk_only) {
     // Re-derive the sample contexts (at0 subtrees) from the node graph: every
     // node reachable only through `at0` belongs to the sample-0 prologue.
     const Plan& P = plan_in;
@@ -844,10 +845,12 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
 
     const int vec = effective_vec(P, low);
     std::ostringstream o;
-    o << "// generated by aether_gb300 from an aether-ir/1 plan\n";
-    o << "#include \"ag_device.cuh\"\n";
-    if (low.math >= 1) o << "#include \"ag_emu64.cuh\"\n";
-    o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
+    if (!chunk_only) {
+        o << "// generated by aether_gb300 from an aether-ir/1 plan\n";
+        o << "#include \"ag_device.cuh\"\n";
+        if (low.math >= 1) o << "#include \"ag_emu64.cuh\"\n";
+        o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
+    }
     const std::string W = g.W, S = g.S;
     const int OC = P.dst_comps * (dst_ff ? 2 : 1);   // stored planes (ff: hi planes, then lo planes)
     const bool sum = P.wants_sum(), store = P.wants_store();
@@ -858,7 +861,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         // The native FP64 recomputation of one sample, out of line so its
         // registers do not weigh on the double-float fast path. It reloads its
         // own operands at sample `s` (s < n is checked by the caller).
-        o << "__device__ __noinline__ void ag_native_lane(const AgArgs& a, ag_u64 s, double* fv) {\n";
+        o << "__device__ __noinline__ void ag_native_lane" << suffix << "(const AgArgs& a, ag_u64 s, double* fv) {\n";
         if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n    const ag_u32 g = a.offset + (ag_u32)s;\n";
         o << gn.pro.str() << gn.body.str();
         for (int c = 0; c < P.dst_comps; ++c) o << "    fv[" << c << "] = " << nroot[size_t(c)] << ";\n";
@@ -866,7 +869,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     }
 
     // The chunk body: one pass of a CTA over block*ipt*VEC consecutive samples.
-    o << "template <int VEC>\n__device__ __forceinline__ void ag_chunk(const AgArgs& a, ag_u64 chunk";
+    o << "template <int VEC>\n__device__ __forceinline__ void ag_chunk" << suffix << "(const AgArgs& a, ag_u64 chunk";
     if (sum) o << (prec ? ", ag::e64::df& acc" : ", double& acc_h, double& acc_c");
     o << ") {\n";
     o << "    constexpr int L = AG_IPT * VEC;\n";
@@ -927,7 +930,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         // Samples outside the double-float range are recomputed natively.
         o << "        const ag_u64 sl_ = s0[l / VEC] + (ag_u64)(l % VEC);\n";
         o << "        if (!ok_ && sl_ < a.n) {\n            double nv_[" << P.dst_comps << "];\n";
-        o << "            ag_native_lane(a, sl_, nv_);\n";
+        o << "            ag_native_lane" << suffix << "(a, sl_, nv_);\n";
         for (int c = 0; c < P.dst_comps; ++c)
             o << "            fv" << c << " = " << (prec ? "ag::e64::dfc(nv_[" + std::to_string(c) + "])" : "nv_[" + std::to_string(c) + "]") << ";\n";
         o << "        }\n";
@@ -964,6 +967,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     }
     o << "}\n";
 
+    if (chunk_only) return o.str();
     std::ostringstream k;
     k << o.str();
     const std::string lb = low.min_blocks > 0 ? "__launch_bounds__(AG_BLOCK, " + std::to_string(low.min_blocks) + ")"
@@ -990,6 +994,54 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         k << "    }\n}\n";
     }
     return k.str();
+}
+
+}  // namespace ag
+
+namespace ag {
+
+std::string generate_batch_source(const std::vector<const Plan*>& plans, const std::vector<Lowering>& lows,
+                                  int block, int ipt, const std::string& base) {
+    std::ostringstream o;
+    bool emu = false;
+    for (const Lowering& l : lows) emu = emu || l.math >= 1;
+    o << "// generated by aether_gb300: batch of " << plans.size() << " plans\n";
+    o << "#include \"ag_device.cuh\"\n";
+    if (emu) o << "#include \"ag_emu64.cuh\"\n";
+    o << "#define AG_BLOCK " << block << "\n#define AG_IPT " << ipt << "\n";
+    std::vector<int> vecs;
+    for (size_t p = 0; p < plans.size(); ++p) {
+        if (plans[p]->wants_sum()) throw std::runtime_error("aether-ir: sum plans cannot join a batch");
+        Lowering l = lows[p];
+        l.block = block;
+        l.ipt = ipt;
+        vecs.push_back(effective_vec(*plans[p], l));
+        o << generate_source(*plans[p], l, base, "_p" + std::to_string(p), true);
+    }
+    // The work list: one argument block per item, the first global tile of the
+    // item, and the plan it runs. Items are sorted by tile0.
+    o << "struct AgItem {\n    AgArgs a;\n    ag_u64 tile0;\n    int plan;\n    int pad;\n};\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(AG_BLOCK) " << base
+      << "(const AgItem* __restrict__ items, int n_items, ag_u64 total_tiles) {\n";
+    o << "    __shared__ int s_item;\n";
+    o << "    for (ag_u64 t = blockIdx.x; t < total_tiles; t += gridDim.x) {\n";
+    o << "        if (threadIdx.x == 0) {\n";
+    o << "            int lo = 0, hi = n_items - 1;\n";
+    o << "            while (lo < hi) {\n";
+    o << "                const int mid = (lo + hi + 1) >> 1;\n";
+    o << "                if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1;\n";
+    o << "            }\n";
+    o << "            s_item = lo;\n";
+    o << "        }\n";
+    o << "        __syncthreads();\n";
+    o << "        const AgItem& it = items[s_item];\n";
+    o << "        __syncthreads();\n";
+    o << "        const ag_u64 ch = t - it.tile0;\n";
+    o << "        switch (it.plan) {\n";
+    for (size_t p = 0; p < plans.size(); ++p)
+        o << "        case " << p << ": ag_chunk_p" << p << "<" << vecs[p] << ">(it.a, ch); break;\n";
+    o << "        default: break;\n        }\n    }\n}\n";
+    return o.str();
 }
 
 }  // namespace ag

@@ -59,8 +59,18 @@ const char* dtype_name(DType d);
 int dtype_size(DType d);
 
 // Generated CUDA source for the plan: kernels `<base>_v` (vectorized lane
-// groups) and `<base>_s` (one sample per lane group).
-std::string generate_source(const Plan& plan, const Lowering& low, const std::string& base = "ag_plan");
+// groups) and `<base>_s` (one sample per lane group). With chunk_only, only
+// the per-chunk device function `ag_chunk<suffix>` (and its fallback) is
+// emitted, for inclusion in a batch module.
+std::string generate_source(const Plan& plan, const Lowering& low, const std::string& base = "ag_plan",
+                            const std::string& suffix = "", bool chunk_only = false);
+
+// One persistent kernel `<base>` over a device work list of items, each an
+// argument block plus the plan it runs; items are cut into tiles of
+// block*ipt*vec_p samples that CTAs take round-robin. All plans share block
+// and ipt; each keeps its own math mode and vector width.
+std::string generate_batch_source(const std::vector<const Plan*>& plans, const std::vector<Lowering>& lows,
+                                  int block, int ipt, const std::string& base);
 
 // Kernel base name of a plan: ag_<expr|fill|sum>_<8 hex digits of the text hash>,
 // so profiles and launch lists tell plans apart.

@@ -166,6 +166,132 @@ def run_reference(args):
     return 0
 
 
+def _time_ms(fn, reps=5, warmup=2):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def secondary_config1(ag):
+    """Config 1: d = a + b*c + sin(a)*exp(-c*c), Array<double,3>, 2^20 samples."""
+    n = 1 << 20
+    g = ag.Generator(42)
+    arrs = [ag.Array("f64", (3,), n) for _ in range(3)]
+    for k, x in enumerate(arrs):
+        ag.assign(x, g.substream(k).uniform(3, -1.0, 1.0))
+    a, b, c = (x.view() for x in arrs)
+    d = ag.Array("f64", (3,), n)
+    e = a + b * c + ag.cwiseSin(a) * ag.cwiseExp((c * c) * (-1.0))
+    out = {"samples": n, "bytes_per_sample": 96}
+    for name, m in (("native", 0), ("emulated", 1)):
+        L = ag.prepare(d, e, math=m, tune=True)
+        ms = _time_ms(L, reps=20)
+        out[name] = {"ms": round(ms, 4), "gbs": round(n * 96 / (ms * 1e-3) / 1e9, 1)}
+    return out
+
+
+def secondary_config3(ag, n=1 << 27):
+    """Config 3 (precision form): per-sample dot of two Array<float,8> plus one
+    global sum, FP32 storage with float-float working values, against the same
+    workload in FP64 storage (best of the native and emulated FP64 lowerings)."""
+    import torch
+    g = ag.Generator(3)
+
+    def loguniform(arr, k):
+        sign = g.substream(2 * k).bernoulli(8, 0.5) * 2.0 - 1.0
+        mag = ag.cwiseExp(g.substream(2 * k + 1).uniform(8, -6.0, 6.0) * 2.302585092994046)
+        ag.assign(arr, sign * mag)
+
+    x32, y32 = ag.Array("f32", (8,), n), ag.Array("f32", (8,), n)
+    loguniform(x32, 0)
+    loguniform(y32, 1)
+    d32 = ag.Array("f32", (1,), n)
+    red32 = torch.zeros(2, dtype=torch.float64, device="cuda")
+    L32 = ag.prepare(d32, x32.view().dot(y32.view()), op="setsum", reduce_out=red32, math=2, tune=True)
+    ms32 = _time_ms(L32)
+    # the same FP32 values widened to FP64 storage
+    x64, y64 = ag.Array("f64", (8,), n), ag.Array("f64", (8,), n)
+    x64.data.copy_(x32.data)
+    y64.data.copy_(y32.data)
+    del x32, y32
+    d64 = ag.Array("f64", (1,), n)
+    red64 = torch.zeros(2, dtype=torch.float64, device="cuda")
+    res = {"samples": n, "bytes_per_sample_f32": 68, "bytes_per_sample_f64": 136,
+           "ff_ms": round(ms32, 4), "ff_samples_per_s": round(n / (ms32 * 1e-3), 1)}
+    best = None
+    for name, m in (("f64_native", 0), ("f64_emulated", 1)):
+        L64 = ag.prepare(d64, x64.view().dot(y64.view()), op="setsum", reduce_out=red64, math=m, tune=True)
+        ms = _time_ms(L64)
+        res[name + "_ms"] = round(ms, 4)
+        best = ms if best is None else min(best, ms)
+    torch.cuda.synchronize()
+    # agreement of the two forms on this workload (per-sample and global sum)
+    a32 = d32.data[0, :n].double()
+    a64 = d64.data[0, :n]
+    scale = torch.sum(torch.abs(x64.data[:, :n] * y64.data[:, :n]), dim=0)
+    res["max_rel_diff_f32_out_vs_f64"] = float(torch.max(torch.abs(a32 - a64) / scale).item())
+    s32, s64 = red32.cpu().tolist(), red64.cpu().tolist()
+    res["global_sum_rel_diff"] = abs((s32[0] + s32[1]) - (s64[0] + s64[1])) / abs(s64[0] + s64[1])
+    res["speedup_vs_fp64"] = round(best / ms32, 3)
+    res["gbs_ff"] = round(n * 68 / (ms32 * 1e-3) / 1e9, 1)
+    return res
+
+
+def config4_workload(ag, n_items=4096, median=4096, sigma=1.5, lo=64, hi=1 << 21, seed=4, math=1):
+    """Config 4: uneven arrays cycling cross product (Vec3d), quaternion rotate
+    and the guarded 3x3 inverse; lognormal sizes."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.round(rng.lognormal(np.log(median), sigma, n_items)), lo, hi).astype(int)
+    g = ag.Generator(seed)
+    launches, keep, nbytes = [], [], 0
+    for i, n in enumerate(sizes):
+        gi = g.substream(i)
+        if i % 3 == 0:
+            a, b, out = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
+            ag.assign(a, gi.substream(0).uniform(3, -1.0, 1.0))
+            ag.assign(b, gi.substream(1).uniform(3, -1.0, 1.0))
+            e, bps, ins = a.view().cross(b.view()), 72, (a, b)
+        elif i % 3 == 1:
+            q, v, out = ag.Array("f64", (4,), n), ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
+            ag.assign(q, gi.substream(0).uniform(4, -1.0, 1.0))
+            ag.assign(v, gi.substream(1).uniform(3, -1.0, 1.0))
+            e, bps, ins = q.view().quatRotate(v.view()), 80, (q, v)
+        else:
+            m, out = ag.Array("f64", (3, 3), n), ag.Array("f64", (3, 3), n)
+            ag.assign(m, gi.substream(0).uniform(9, -1.0, 1.0).reshape((3, 3)))
+            M = m.view()
+            e, bps, ins = ag.select(ag.cwiseAbs(M.det()) > 1e-300, M.inverse(), ag.constant(0.0, (3, 3))), 144, (m,)
+        launches.append(ag.prepare(out, e, math=math))
+        keep.append((out, ins))
+        nbytes += int(n) * bps
+    return launches, keep, nbytes, sizes
+
+
+def secondary_config4(ag):
+    import torch
+    launches, keep, nbytes, sizes = config4_workload(ag)
+    batch = ag.Batch(launches, block=256)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        each_ms = _time_ms(batch.launch_each, reps=3, warmup=1)
+        batch_ms = _time_ms(batch.launch, reps=5)
+        batch.capture(s.cuda_stream)
+        graph_ms = _time_ms(lambda: batch.replay(s.cuda_stream), reps=5)
+    return {"items": len(launches), "samples": int(sizes.sum()), "bytes": nbytes,
+            "per_call_ms": round(each_ms, 3), "batch_ms": round(batch_ms, 3), "graph_ms": round(graph_ms, 3),
+            "speedup_batch": round(each_ms / batch_ms, 2), "speedup_graph": round(each_ms / graph_ms, 2),
+            "gbs_graph": round(nbytes / (graph_ms * 1e-3) / 1e9, 1), "math": "emulated FP64"}
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -284,6 +410,16 @@ def run_ours(args):
     if not args.no_cpu:
         gbs, t, nt, sample = cpu_leg(1, 1)
         cpu = {"value": round(gbs, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample}
+    secondary = None
+    if not args.no_secondary:
+        # the other configurations, measured after the timed region
+        secondary = {}
+        for name, fn in (("config1_plain", secondary_config1), ("config3_precision_form", secondary_config3),
+                         ("config4_batch", secondary_config4)):
+            try:
+                secondary[name] = fn(ag)
+            except Exception as ex:   # reported, never hidden
+                secondary[name] = {"error": str(ex).splitlines()[0][:300] if str(ex) else repr(ex)}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
@@ -296,7 +432,7 @@ def run_ours(args):
                                      "vec": k_fill.plan.info().vec, "registers": k_fill.plan.info().registers},
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
+        "gpu_launches": 2 * args.steps, "clocks": clk.summary(), "secondary": secondary,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -314,6 +450,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default lowering instead of the autotuned one")
+    ap.add_argument("--no-secondary", action="store_true", help="skip configs 1, 3 and 4 after the timed region")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
     args = ap.parse_args()

@@ -128,6 +128,48 @@ int aether_plan_launch(void* plan, const AetherLaunch* args, void* stream);
 int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len);
 void aether_plan_release(void* plan);
 
+/* ------------------------------------------------------------------------- *
+ * Batches: many independent assignments (arrays of uneven sizes, several
+ * expression kinds) as one persistent kernel over a device work list, and
+ * that launch captured into a CUDA graph. Replaces a host loop of
+ * consumer-written kernel launches, one per array (backend/cuda/Launch.h:53-88,
+ * the pattern of tests/test_GraphCapture.cu:50-57), whose capture rules
+ * (tests/test_GraphCapture.cu:17-25) the capture below follows. Sum plans
+ * cannot join a batch.
+ * ------------------------------------------------------------------------- */
+typedef struct AetherBatchItem {
+    int plan;          /* index into the plans given to aether_batch_create */
+    int reserved;
+    AetherLaunch args; /* as for aether_plan_launch; every plane 16-byte aligned */
+} AetherBatchItem;
+
+typedef struct AetherBatchInfo {
+    uint64_t hash;
+    int n_plans, n_items;
+    uint64_t total_tiles;
+    int block, ipt;
+    int registers, blocks_per_sm;
+    double compile_ms;
+} AetherBatchInfo;
+
+/* Compile one persistent kernel for `plans` (block/ipt from `lowering`). */
+int aether_batch_create(void* const* plans, int n_plans, const AetherLowering* lowering, void** batch);
+/* Replace the work list; items are cut into equal tiles the CTAs take
+ * round-robin. Returns once the list is on the device. */
+int aether_batch_set_items(void* batch, const AetherBatchItem* items, int n_items, void* stream);
+/* One launch over the whole work list. */
+int aether_batch_launch(void* batch, void* stream);
+/* Capture one launch into a CUDA graph held by the batch (non-default stream);
+ * aether_batch_replay launches it. A work list with a different tiling needs a
+ * new capture; new contents with the same tiling do not. */
+int aether_batch_capture(void* batch, void* stream);
+int aether_batch_replay(void* batch, void* stream);
+int aether_batch_info(void* batch, AetherBatchInfo* info);
+void aether_batch_release(void* batch);
+/* `count` plain launches from one host loop: the per-call baseline a batch is
+ * measured against. */
+int aether_plan_launch_many(void* const* plans, const AetherLaunch* args, int count, void* stream);
+
 /* Launch a sum plan without allocating anything on the device. No counterpart
  * in the reference: it exists for callers that cannot call cudaMalloc where
  * they launch -- work being recorded into a CUDA graph, hosts that run under a
