@@ -50,6 +50,37 @@ class AetherBatchInfo(ctypes.Structure):
                 ("registers", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("compile_ms", ctypes.c_double)]
 
 
+class AetherServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("mode", ctypes.c_int), ("max_inflight", ctypes.c_int),
+                ("max_items", ctypes.c_int), ("block", ctypes.c_int), ("ipt", ctypes.c_int),
+                ("idle_spin_us", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class AetherServeOperand(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("host", ctypes.c_void_p), ("pitch", ctypes.c_uint64)]
+
+
+class AetherServeRequest(ctypes.Structure):
+    _fields_ = [("plan", ctypes.c_int), ("flags", ctypes.c_int), ("n", ctypes.c_uint64),
+                ("operands", ctypes.POINTER(AetherServeOperand)), ("n_operands", ctypes.c_uint32),
+                ("n_scalars", ctypes.c_uint32), ("scalars", ctypes.POINTER(ctypes.c_double)),
+                ("keys", ctypes.POINTER(ctypes.c_uint64)), ("n_keys", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("host_out", ctypes.c_void_p), ("arrival_ns", ctypes.c_uint64)]
+
+
+class AetherServeStatus(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("launch_items", ctypes.c_int), ("t_arrival_ns", ctypes.c_uint64),
+                ("t_dispatch_ns", ctypes.c_uint64), ("t_done_ns", ctypes.c_uint64), ("output", ctypes.c_void_p),
+                ("out_pitch", ctypes.c_uint64), ("bytes", ctypes.c_uint64), ("uploaded_bytes", ctypes.c_uint64)]
+
+
+class AetherServeStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint64) for name in (
+        "submitted", "completed", "failed", "launches", "launched_items", "bytes", "uploaded_bytes",
+        "resident_hits", "resident_misses", "evictions", "arena_bytes", "arena_peak_bytes", "resident_bytes",
+        "first_arrival_ns", "last_done_ns", "enqueue_ns")]
+
+
 # name -> (restype, argtypes); every symbol include/aether_gb300.h declares.
 _P = ctypes.c_void_p
 _SIGS = {
@@ -81,6 +112,16 @@ _SIGS = {
     "aether_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(AetherBatchInfo)]),
     "aether_batch_release": (None, [_P]),
     "aether_plan_launch_many": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(AetherLaunch), ctypes.c_int, _P]),
+    "aether_serve_open": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(AetherServeConfig),
+                                         ctypes.POINTER(_P)]),
+    "aether_serve_submit": (ctypes.c_int, [_P, ctypes.POINTER(AetherServeRequest), ctypes.POINTER(ctypes.c_uint64)]),
+    "aether_serve_feed": (ctypes.c_int, [_P, ctypes.POINTER(AetherServeRequest), ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_uint64)]),
+    "aether_serve_status": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(AetherServeStatus)]),
+    "aether_serve_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(AetherServeStatus)]),
+    "aether_serve_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "aether_serve_stats": (ctypes.c_int, [_P, ctypes.POINTER(AetherServeStats)]),
+    "aether_serve_close": (None, [_P]),
     "aether_plan_generate": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.c_char_p,
                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_nvrtc_check": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),

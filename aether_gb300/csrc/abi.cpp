@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "internal.h"
 #include "jit.h"
 #include "plan.h"
 
@@ -105,44 +106,6 @@ bool capturing(cudaStream_t s) {
 // Plans.
 // ---------------------------------------------------------------------------
 
-// Host image of the device's AgArgs (csrc/device/ag_device.cuh); the kernel
-// receives it by value.
-struct AgArgsHost {
-    uint64_t n;
-    uint32_t offset, flags;
-    char* dst;
-    uint64_t dst_pitch;
-    const char* ops[16];
-    uint64_t pitch[16];
-    double sc[16];
-    float sch[16];
-    float scl[16];
-    uint64_t key[8];
-    double* red;
-    char* ws;
-    uint64_t ws_bytes;
-};
-static_assert(sizeof(AgArgsHost) == 632, "AgArgs layout");
-
-struct PlanObj {
-    ag::Plan plan;
-    ag::Lowering low;
-    std::string name;
-    std::string source;
-    ag::Compiled compiled;
-    cudaLibrary_t library = nullptr;
-    cudaKernel_t fv = nullptr, fs = nullptr;
-    int vec = 2;
-    int registers = 0;
-    int blocks_per_sm_v = 1, blocks_per_sm_s = 1;
-    int sms = 1;
-    int dev = 0;
-    // default workspace of sum plans
-    std::mutex ws_mu;
-    void* ws = nullptr;
-    size_t ws_bytes = 0;
-};
-
 ag::Lowering default_lowering(const ag::Plan& p) {
     ag::Lowering l;
     l.block = 256;
@@ -152,10 +115,6 @@ ag::Lowering default_lowering(const ag::Plan& p) {
     l.math = 0;
     (void)p;
     return l;
-}
-
-uint64_t chunk_samples(const PlanObj& P, bool vectorized) {
-    return uint64_t(P.low.block) * uint64_t(P.low.ipt) * uint64_t(vectorized ? P.vec : 1);
 }
 
 uint64_t ws_needed(const PlanObj& P, uint64_t n) {
@@ -401,9 +360,7 @@ AG_EXPORT int aether_plan_source(void* plan, char* buf, size_t cap, size_t* len)
 // through aether_last_error.
 int ag_internal_fail(const char* message) { return fail(message); }
 
-// Validate a launch against its plan and build the kernel's argument block.
-// Returns whether every plane is 16-byte aligned (the vectorized kernel).
-static bool make_args(const PlanObj* P, const AetherLaunch* a, AgArgsHost& k) {
+bool make_args(const PlanObj* P, const AetherLaunch* a, AgArgsHost& k) {
     const ag::Plan& pl = P->plan;
     if (a->n > 0xFFFFFFFFull) throw std::runtime_error("plan_launch: n exceeds the 32-bit sample index");
     if (uint64_t(a->sample_offset) + a->n - 1 > 0xFFFFFFFFull)
@@ -498,38 +455,9 @@ AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream
 // ============================================================================
 namespace {
 
-struct AgItemHost {
-    AgArgsHost a;
-    uint64_t tile0;
-    int plan;
-    int pad;
-};
-static_assert(sizeof(AgItemHost) == 648, "AgItem layout");
-
-struct BatchObj {
-    std::vector<PlanObj*> plans;
-    std::vector<int> vecs;
-    int block = 256, ipt = 1;
-    std::string name, source;
-    ag::Compiled compiled;
-    cudaLibrary_t library = nullptr;
-    cudaKernel_t kernel = nullptr;
-    int blocks_per_sm = 1, sms = 1, registers = 0;
-    AgItemHost* host_items = nullptr;   // pinned staging of the work list
-    void* dev_items = nullptr;
-    size_t cap_items = 0;
-    int n_items = 0;
-    uint64_t total_tiles = 0;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    uint64_t graph_tiles = 0;
-    int graph_items = 0;
-};
-
 void batch_enqueue(BatchObj* B, cudaStream_t s) {
     if (B->total_tiles == 0) return;
-    const uint64_t cap = uint64_t(std::max(B->blocks_per_sm, 1)) * uint64_t(B->sms);
-    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min(B->total_tiles, cap)));
+    const unsigned grid = batch_grid(*B, B->total_tiles);
     void* items = B->dev_items;
     int n = B->n_items;
     uint64_t tiles = B->total_tiles;
@@ -618,7 +546,7 @@ AG_EXPORT int aether_batch_set_items(void* batch, const AetherBatchItem* items, 
                                          " has a plane that is not 16-byte aligned");
             h.tile0 = tiles;
             h.plan = it.plan;
-            const uint64_t per = uint64_t(B->block) * uint64_t(B->ipt) * uint64_t(B->vecs[size_t(it.plan)]);
+            const uint64_t per = batch_tile_samples(*B, it.plan);
             tiles += (it.args.n + per - 1) / per;
         }
         B->n_items = n_items;

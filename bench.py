@@ -292,6 +292,56 @@ def secondary_config4(ag):
             "gbs_graph": round(nbytes / (graph_ms * 1e-3) / 1e9, 1), "math": "emulated FP64"}
 
 
+SERVE_RATES = (1000, 2000, 5000, 10000, 20000, 50000)
+
+
+def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, saturation_requests=20000):
+    """Mixed serving: Poisson arrivals of the eight standard shapes, lognormal
+    sizes (median 65,536, sigma 1, clipped to [1,024, 4,194,304]), operands
+    reused with p = 0.7 and copied in from pinned host memory otherwise, a
+    120 GB arena. Each rate runs the same trace through continuous batching
+    and through one plain launch per request; latency is arrival (scheduled)
+    to completion seen by the host, over all but the first 10% of requests.
+    Saturation: every request arrives at time 0."""
+    from aether_gb300 import serve
+    shapes = serve.standard_shapes()
+    pools = serve.HostPools()
+
+    def run(mode, trace):
+        with serve.Server(shapes, budget, mode=mode) as srv:
+            reqs = []
+            for s, n, ids, t in trace:
+                sh = shapes[s]
+                hosts = [pools.window(dt, i, sh.operand_bytes(k, n)) for k, ((dt, _), i) in enumerate(zip(sh.operands, ids))]
+                reqs.append(srv.request(s, n, ids, hosts, arrival_ns=t))
+            sts = srv.wait_all(srv.feed(reqs))
+            st = srv.stats()
+        span = (st["last_done_ns"] - st["first_arrival_ns"]) * 1e-9
+        samples = sum(n for _, n, _, _ in trace)
+        out = {"requests": len(trace), "req_per_s": round(len(trace) / span, 1),
+               "samples_per_s": round(samples / span, 1), "gbs": round(st["bytes"] / span / 1e9, 1),
+               "launches": st["launches"], "items_per_launch": round(st["launched_items"] / max(1, st["launches"]), 2),
+               "resident_hit_rate": round(st["resident_hits"] / max(1, st["resident_hits"] + st["resident_misses"]), 3),
+               "uploaded_gb": round(st["uploaded_bytes"] / 1e9, 2), "evictions": st["evictions"],
+               "enqueue_us_per_launch": round(st["enqueue_ns"] / 1e3 / max(1, st["launches"]), 2),
+               "arena_peak_gb": round(st["arena_peak_bytes"] / 1e9, 1), "failed": st["failed"]}
+        out.update(serve.latency_summary(sts[len(sts) // 10:]))
+        return out
+
+    res = {"shapes": [s.name for s in shapes], "budget_bytes": budget, "reuse": 0.7,
+           "sizes": "lognormal median 65536 sigma 1.0 clipped [1024, 4194304]",
+           "latency": "scheduled arrival to completion seen by the host", "outputs": "left in HBM", "rates": {}}
+    for i, rate in enumerate(rates):
+        n = int(min(60000, max(1000, rate * seconds)))
+        trace = serve.make_trace(shapes, n, float(rate), seed=100 + i)
+        res["rates"][str(rate)] = {"batched": run("batched", trace), "plain": run("plain", trace)}
+    for name, reuse in (("saturation", 0.7), ("saturation_resident", 1.0)):
+        trace = serve.make_trace(shapes, saturation_requests, None, seed=7, reuse=reuse)
+        b, p = run("batched", trace), run("plain", trace)
+        res[name] = {"batched": b, "plain": p, "speedup_req_per_s": round(b["req_per_s"] / p["req_per_s"], 2)}
+    return res
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -415,7 +465,7 @@ def run_ours(args):
         # the other configurations, measured after the timed region
         secondary = {}
         for name, fn in (("config1_plain", secondary_config1), ("config3_precision_form", secondary_config3),
-                         ("config4_batch", secondary_config4)):
+                         ("config4_batch", secondary_config4), ("config5_serving", secondary_config5)):
             try:
                 secondary[name] = fn(ag)
             except Exception as ex:   # reported, never hidden

@@ -183,6 +183,103 @@ int aether_plan_launch_many(void* const* plans, const AetherLaunch* args, int co
  * overlap on the GPU race and must be serialised by the caller. */
 int aether_plan_launch_noalloc(void* plan, const AetherLaunch* args, void* stream);
 
+/* ------------------------------------------------------------------------- *
+ * Serving: a request loop with continuous batching. No single counterpart in
+ * the reference: it serves, from one process, what a reference user gets
+ * from one assignment per call (expr/Assign.h:251-346 through
+ * backend/cuda/Launch.h:53-88, synchronised per call) on arrays kept on the
+ * device (a device copy of host bytes, residency/Replica.h:56-100, filled by
+ * chunk/Copy.h:87-192).
+ *
+ * The server owns one device arena of `hbm_budget_bytes`. Every request names
+ * its operands by a residency id: an id already on the device is reused, a
+ * new one is copied in from its host bytes, and idle operands are evicted
+ * least recently used first when the arena is full. A request is admitted
+ * when its output and its missing operands fit in the arena; requests wait in
+ * arrival order until they do. Admitted requests that arrive while others run
+ * are launched as soon as one of `max_inflight` launch slots frees up, up to
+ * `max_items` requests per launch in one persistent batched kernel
+ * (AETHER_SERVE_BATCHED), or one plain plan launch each
+ * (AETHER_SERVE_PLAIN, the per-call baseline). Results do not depend on the
+ * mode or on the mix: each request runs its plan's own arithmetic.
+ * ------------------------------------------------------------------------- */
+enum { AETHER_SERVE_BATCHED = 0, AETHER_SERVE_PLAIN = 1 };
+/* request flags */
+enum { AETHER_SERVE_KEEP_OUTPUT = 1 };
+/* request states */
+enum { AETHER_SERVE_QUEUED = 0, AETHER_SERVE_RUNNING = 1, AETHER_SERVE_DONE = 2, AETHER_SERVE_FAILED = 3 };
+
+typedef struct AetherServeConfig {
+    uint64_t hbm_budget_bytes; /* size of the device arena (operands + outputs) */
+    int mode;                  /* AETHER_SERVE_BATCHED or AETHER_SERVE_PLAIN */
+    int max_inflight;          /* launches on the device at once; 0 = 4 */
+    int max_items;             /* requests per batched launch; 0 = 256 */
+    int block, ipt;            /* lowering of the batched kernel; 0 = 512, 1 */
+    int idle_spin_us;          /* the loop polls this long after its last work before it sleeps; 0 = 2000 */
+    int reserved;
+} AetherServeConfig;
+
+typedef struct AetherServeOperand {
+    uint64_t id;      /* residency key: equal ids name equal bytes */
+    const void* host; /* the bytes (pinned memory copies fastest); may be NULL if the id is resident */
+    uint64_t pitch;   /* samples per plane (0 = n); pitch * element size a multiple of 16 */
+} AetherServeOperand;
+
+typedef struct AetherServeRequest {
+    int plan;                            /* index into the plans given to aether_serve_open */
+    int flags;                           /* AETHER_SERVE_KEEP_OUTPUT */
+    uint64_t n;                          /* samples */
+    const AetherServeOperand* operands;  /* one per plan operand, in plan order */
+    uint32_t n_operands;
+    uint32_t n_scalars;
+    const double* scalars;
+    const uint64_t* keys;
+    uint32_t n_keys;
+    uint32_t reserved;
+    void* host_out;       /* optional: the output planes are copied here (comps * out_pitch elements) */
+    uint64_t arrival_ns;  /* aether_serve_feed: arrival time after the feed starts */
+} AetherServeRequest;
+
+typedef struct AetherServeStatus {
+    int state;            /* AETHER_SERVE_* state */
+    int launch_items;     /* requests in the launch that ran this one */
+    uint64_t t_arrival_ns, t_dispatch_ns, t_done_ns; /* since aether_serve_open */
+    const void* output;   /* device output while kept (AETHER_SERVE_KEEP_OUTPUT) */
+    uint64_t out_pitch;   /* samples per output plane */
+    uint64_t bytes;       /* algorithmic bytes: operand planes read + output planes written */
+    uint64_t uploaded_bytes; /* operand bytes this request copied in */
+} AetherServeStatus;
+
+typedef struct AetherServeStats {
+    uint64_t submitted, completed, failed;
+    uint64_t launches, launched_items;
+    uint64_t bytes, uploaded_bytes;
+    uint64_t resident_hits, resident_misses, evictions;
+    uint64_t arena_bytes, arena_peak_bytes, resident_bytes;
+    uint64_t first_arrival_ns, last_done_ns;
+    uint64_t enqueue_ns;      /* host time the loop spent issuing copies and launches */
+} AetherServeStats;
+
+/* Compile the batched kernel for `plans` (none may be a sum plan), allocate the
+ * arena and start the loop's thread on the calling thread's device. */
+int aether_serve_open(void* const* plans, int n_plans, const AetherServeConfig* config, void** server);
+/* Queue one request now; its ticket identifies it until aether_serve_release
+ * (kept outputs) or aether_serve_close. Requests that can never fit the arena
+ * or do not match their plan are refused here. */
+int aether_serve_submit(void* server, const AetherServeRequest* request, uint64_t* ticket);
+/* Queue `count` requests, each at its arrival_ns after the call starts
+ * (sleeping or spinning in between on the calling thread); the arrival time
+ * recorded is the scheduled one. tickets[i] receives request i's ticket. */
+int aether_serve_feed(void* server, const AetherServeRequest* requests, int count, uint64_t* tickets);
+int aether_serve_status(void* server, uint64_t ticket, AetherServeStatus* status);
+/* Wait until the request is done or failed, or `timeout_s` passes (status 1). */
+int aether_serve_wait(void* server, uint64_t ticket, double timeout_s, AetherServeStatus* status);
+/* Free a kept output. */
+int aether_serve_release(void* server, uint64_t ticket);
+int aether_serve_stats(void* server, AetherServeStats* stats);
+/* Finish the work on the device, stop the loop and free the arena. */
+void aether_serve_close(void* server);
+
 /* Offline lowering, no device needed: parse and check `ir`, write the CUDA
  * source of its kernel into `buf` (up to `cap` bytes, NUL-terminated) and its
  * length into `len`. Stands in for the reference's compile-time type check of
