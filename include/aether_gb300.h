@@ -66,7 +66,7 @@ int aether_stream_sync(int dev, void* stream);
  * its launch (backend/cuda/Launch.h:53-74 launchConfig, :84-88
  * checkLastLaunch), and the bundle variant (backend/cuda/bundle/Assign.h:55-268,
  * bundle/LoadStore.h:149-318). The expression is the aether-ir/1 text that
- * the C++ front end (aether_gb300/include/aether) serialises from the
+ * the C++ front end (the headers under include/aether) serialises from the
  * expression tree's type; the kernel is compiled once per (text, lowering)
  * and cached in memory and on disk by hash.
  * ------------------------------------------------------------------------- */
@@ -283,7 +283,7 @@ void aether_serve_close(void* server);
 /* Offline lowering, no device needed: parse and check `ir`, write the CUDA
  * source of its kernel into `buf` (up to `cap` bytes, NUL-terminated) and its
  * length into `len`. Stands in for the reference's compile-time type check of
- * an expression (the static_asserts of expr/nodes/*.h and expr/Assign.h:205-231). */
+ * an expression (the static_asserts of the expr/nodes headers and expr/Assign.h:205-231). */
 int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* buf, size_t cap, size_t* len);
 /* Compile `source` with NVRTC for `arch` (e.g. "sm_103a") without loading it;
  * on failure the compiler log is the last error. */
