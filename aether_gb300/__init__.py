@@ -308,8 +308,10 @@ class Batch:
             pass
 
 
+from .runtime import RuntimeOp, runtime_eval, runtime_view  # noqa: E402
+
 __all__ = [
-    "Batch",
+    "Batch", "RuntimeOp", "runtime_eval", "runtime_view",
     "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
     "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
     "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",

@@ -81,6 +81,12 @@ class AetherServeStats(ctypes.Structure):
         "first_arrival_ns", "last_done_ns", "enqueue_ns")]
 
 
+class AetherRuntimeView(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("dtype_code", ctypes.c_uint8), ("dtype_bits", ctypes.c_uint8),
+                ("dtype_lanes", ctypes.c_uint16), ("rank", ctypes.c_int32),
+                ("extents", ctypes.c_int64 * 6), ("strides", ctypes.c_int64 * 6)]
+
+
 # name -> (restype, argtypes); every symbol include/aether_gb300.h declares.
 _P = ctypes.c_void_p
 _SIGS = {
@@ -122,6 +128,9 @@ _SIGS = {
     "aether_serve_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "aether_serve_stats": (ctypes.c_int, [_P, ctypes.POINTER(AetherServeStats)]),
     "aether_serve_close": (None, [_P]),
+    "aether_runtime_eval": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(AetherRuntimeView),
+                                           ctypes.POINTER(AetherRuntimeView), ctypes.POINTER(AetherRuntimeView),
+                                           ctypes.c_double, _P]),
     "aether_plan_generate": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.c_char_p,
                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_nvrtc_check": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),

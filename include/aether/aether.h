@@ -22,6 +22,7 @@
 #include "aether/expr.h"
 #include "aether/math.h"
 #include "aether/random.h"
+#include "aether/runtime.h"
 
 namespace aether {
 inline constexpr int version_major = 0;

@@ -280,6 +280,41 @@ int aether_serve_stats(void* server, AetherServeStats* stats);
 /* Finish the work on the device, stop the loop and free the arena. */
 void aether_serve_close(void* server);
 
+/* ------------------------------------------------------------------------- *
+ * Runtime-typed strided evaluation. Replaces aether::eval::runtimeEval
+ * (eval/Runtime.h:73-300) over RuntimeView descriptors (view/RuntimeView.h:
+ * 71-110): out = op(a, b, scalar) for every element of out's logical shape,
+ * row-major over out's extents, each operand addressed through its own
+ * element strides. Assign copies or casts (double <-> float); the other ops
+ * need one dtype throughout; the scalar is rounded to the input type first.
+ * Every add and multiply rounds on its own. Errors are reported before any
+ * launch, worded as the reference's "<op> failed on <where>, size=<n> bytes
+ * (<detail>)". Operands must be device memory: there is no host path.
+ * ------------------------------------------------------------------------- */
+enum {
+    AETHER_RT_ASSIGN = 0,
+    AETHER_RT_ADD = 1,
+    AETHER_RT_SUB = 2,
+    AETHER_RT_SCALE = 3,
+    AETHER_RT_ADD_SCALED = 4,
+    AETHER_RT_SUB_SCALED = 5
+};
+#define AETHER_RT_RANK_CAP 6
+
+typedef struct AetherRuntimeView {
+    void* data;
+    uint8_t dtype_code;     /* DLPack type code: 2 = float */
+    uint8_t dtype_bits;     /* 32 or 64 */
+    uint16_t dtype_lanes;   /* 1 */
+    int32_t rank;           /* <= AETHER_RT_RANK_CAP */
+    int64_t extents[AETHER_RT_RANK_CAP];
+    int64_t strides[AETHER_RT_RANK_CAP];  /* element units, >= 0 */
+} AetherRuntimeView;
+
+/* `b` is read only by Add, Sub, AddScaled and SubScaled (may be NULL otherwise). */
+int aether_runtime_eval(int op, const AetherRuntimeView* a, const AetherRuntimeView* b, const AetherRuntimeView* out,
+                        double scalar, void* stream);
+
 /* Offline lowering, no device needed: parse and check `ir`, write the CUDA
  * source of its kernel into `buf` (up to `cap` bytes, NUL-terminated) and its
  * length into `len`. Stands in for the reference's compile-time type check of

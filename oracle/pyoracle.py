@@ -162,3 +162,32 @@ def cfg2a(a, b, c, d0, nthreads=0):
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+# ---------------------------------------------------------------------------
+# Runtime-typed strided evaluation (eval/Runtime.h:103-137 evalElement and
+# :221 the scalar cast): numpy restatement over logical-shape views. numpy
+# rounds every float32/float64 add and multiply on its own, as the reference's
+# host loop does under -ffp-contract=off.
+# ---------------------------------------------------------------------------
+RT_ASSIGN, RT_ADD, RT_SUB, RT_SCALE, RT_ADD_SCALED, RT_SUB_SCALED = range(6)
+
+
+def runtime_eval(op, a, b, out_dtype, scalar=0.0):
+    """out = op(a, b, scalar) elementwise; a, b are numpy arrays of out's
+    logical shape (any strides); returns a new array of that shape."""
+    if op == RT_ASSIGN:
+        return np.asarray(a).astype(out_dtype)
+    t = np.asarray(a).dtype.type
+    s = t(scalar)
+    if op == RT_ADD:
+        r = a + b
+    elif op == RT_SUB:
+        r = a - b
+    elif op == RT_SCALE:
+        r = s * a
+    elif op == RT_ADD_SCALED:
+        r = a + s * b
+    else:
+        r = a - s * b
+    return np.asarray(r, dtype=out_dtype)

@@ -38,6 +38,21 @@ int main(int argc, char** argv) {
             std::printf("round trip mismatch at %zu\n", i);
             return 1;
         }
+    // runtime-typed evaluation: cast d to float through its descriptor
+    aether::Array<float, 3> fl(n);
+    aether::eval::runtimeEval(aether::eval::RuntimeOp::Assign, aether::fromView(d.deviceView()), aether::RuntimeView{},
+                              aether::fromView(fl.deviceView()));
+    fl.download();
+    {
+        auto fh = fl.hostView();
+        auto dh = d.hostView();
+        for (std::size_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k)
+                if (fh(k, i) != float(dh(k, i))) {
+                    std::printf("runtimeEval cast mismatch at %zu\n", i);
+                    return 1;
+                }
+    }
     try {
         d.deviceView() = A.dot(B) + aether::constant<aether::extents<2>>(1.0);
         std::printf("shape mismatch was not refused\n");
