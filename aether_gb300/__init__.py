@@ -59,7 +59,7 @@ class Array:
         self.n = int(n)
         if data is not None:
             self.data = data
-            self.capacity = data.shape[1]
+            self.capacity = data.stride(0) if data.shape[0] > 1 else max(data.stride(0), data.shape[1])
         else:
             self.capacity = quantized_capacity(n)
             self.data = _torch().zeros((self.planes, self.capacity), dtype=_tdtype(dtype), device=device)
@@ -78,6 +78,25 @@ class Array:
         shape = shape or (tensor.shape[0],)
         return cls(dtype, shape, n if n is not None else tensor.shape[1], data=tensor)
 
+    @classmethod
+    def from_dlpack(cls, obj, shape=None, n=None):
+        """Zero-copy import of a DLPack-exporting (planes, pitch) buffer
+        (interop/DLPack.h:226-430): any framework's device tensor."""
+        t = _torch().utils.dlpack.from_dlpack(obj)
+        if t.dim() == 1:
+            t = t.reshape(1, -1)
+        if t.dim() != 2 or t.stride(1) != 1:
+            raise AetherError("from_dlpack: need a (planes, pitch) buffer with unit sample stride")
+        return cls.wrap(t, shape=shape, n=n)
+
+    def __dlpack__(self, stream=None):
+        """DLPack export of the (planes, n) samples, plane stride = capacity."""
+        v = self.data[:, : self.n]
+        return v.__dlpack__() if stream is None else v.__dlpack__(stream=stream)
+
+    def __dlpack_device__(self):
+        return self.data.__dlpack_device__()
+
     def samples(self):
         return self.n
 
@@ -95,6 +114,30 @@ class Array:
         t = torch.as_tensor(host).to(self.data.dtype)
         self.data[:, : self.n].copy_(t.reshape(self.comps, self.n))
         return self
+
+
+def padded_block_samples(n, parts, pad_to=32):
+    """Block pitch of a sample-mode partition: ceil(n / parts) rounded up to
+    pad_to (residency/Partition.h:61-72)."""
+    if parts <= 0:
+        raise AetherError("padded_block_samples failed on n/a, size=%d bytes (parts must be > 0)" % n)
+    if pad_to <= 0:
+        raise AetherError("padded_block_samples failed on n/a, size=%d bytes (pad_to must be > 0)" % n)
+    per = (int(n) + parts - 1) // parts
+    return (per + pad_to - 1) // pad_to * pad_to
+
+
+def partition_view(arr, parts, r, pad_to=32):
+    """Block r of `parts` of an array's sample mode (residency/Partition.h:
+    104-168): starts at sample r * padded, holds min(padded, n - r * padded)
+    real samples, same plane pitch, same memory."""
+    if r < 0 or r >= parts:
+        raise AetherError("partition_view failed on cuda:0, size=0 bytes (block index %d >= spec.parts=%d)" % (r, parts))
+    padded = padded_block_samples(arr.n, parts, pad_to)
+    off = r * padded
+    real = max(0, min(padded, arr.n - off))
+    start = min(off, arr.capacity)
+    return Array.wrap(arr.data[:, start:start + real], shape=arr.shape, n=real)
 
 
 class Plan:
@@ -311,7 +354,7 @@ class Batch:
 from .runtime import RuntimeOp, runtime_eval, runtime_view  # noqa: E402
 
 __all__ = [
-    "Batch", "RuntimeOp", "runtime_eval", "runtime_view",
+    "Batch", "RuntimeOp", "runtime_eval", "runtime_view", "padded_block_samples", "partition_view",
     "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
     "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
     "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",

@@ -18,9 +18,11 @@
 #pragma once
 
 #include "aether/array.h"
+#include "aether/device_flag.h"
 #include "aether/eval.h"
 #include "aether/expr.h"
 #include "aether/math.h"
+#include "aether/partition.h"
 #include "aether/random.h"
 #include "aether/runtime.h"
 

@@ -110,3 +110,30 @@ def test_cpp_consumer_on_device(tmp_path, oracle):
     for k in range(3):
         ref = oracle.fill_uniform_f64(oracle.substream_key(k42, k), -1.0, 1.0, 3, n)
         assert np.array_equal(planes[k], ref[:, :n])
+
+
+def test_cpp_partition_algebra(tmp_path):
+    exe = _compile(os.path.join(REPO, "tests", "cpp", "partition_check.cpp"), str(tmp_path / "partition_check"))
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and "partition ok" in r.stdout, r.stdout
+
+
+@pytest.mark.gpu
+def test_cpp_device_flag(tmp_path):
+    """A consumer kernel sets DeviceFlag through DeviceFlagView; the host
+    reads it (sticky), checkAndClear throws once and clears."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("no nvcc")
+    lib = os.path.join(REPO, "aether_gb300", "lib")
+    exe = str(tmp_path / "device_flag")
+    r = subprocess.run([nvcc, "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-I",
+                        os.path.join(REPO, "include"), os.path.join(REPO, "tests", "cpp", "device_flag.cu"),
+                        "-L", lib, "-laether_gb300", "-Xlinker", "-rpath," + lib, "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and "device flag ok" in r.stdout, r.stdout + r.stderr
