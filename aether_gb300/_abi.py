@@ -53,7 +53,7 @@ class AetherBatchInfo(ctypes.Structure):
 class AetherServeConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("mode", ctypes.c_int), ("max_inflight", ctypes.c_int),
                 ("max_items", ctypes.c_int), ("block", ctypes.c_int), ("ipt", ctypes.c_int),
-                ("idle_spin_us", ctypes.c_int), ("reserved", ctypes.c_int)]
+                ("idle_spin_us", ctypes.c_int), ("upload_engine", ctypes.c_int)]
 
 
 class AetherServeOperand(ctypes.Structure):
@@ -78,7 +78,7 @@ class AetherServeStats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in (
         "submitted", "completed", "failed", "launches", "launched_items", "bytes", "uploaded_bytes",
         "resident_hits", "resident_misses", "evictions", "arena_bytes", "arena_peak_bytes", "resident_bytes",
-        "first_arrival_ns", "last_done_ns", "enqueue_ns")]
+        "first_arrival_ns", "last_done_ns", "enqueue_ns", "admit_ns")]
 
 
 class AetherRuntimeView(ctypes.Structure):

@@ -26,6 +26,7 @@
 #include <unordered_map>
 
 #include "internal.h"
+#include "serve_copy.h"
 
 #define AG_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -37,56 +38,72 @@ constexpr uint64_t kArenaAlign = 256;
 
 uint64_t round_up(uint64_t x, uint64_t a) { return (x + a - 1) / a * a; }
 
-// First-fit allocator over one device allocation; free ranges are kept by
-// offset and merged with their neighbours when released.
+// Best-fit allocator over one device allocation: free ranges indexed by
+// offset (to merge neighbours on release) and by size (to find the smallest
+// range that fits in O(log n), whatever the fragmentation).
 class Arena {
 public:
     void init(uint64_t bytes) {
         size_ = bytes;
-        free_.clear();
-        free_[0] = bytes;
+        by_off_.clear();
+        by_size_.clear();
+        insert_(0, bytes);
         used_ = peak_ = 0;
     }
     static uint64_t span(uint64_t bytes) { return round_up(bytes ? bytes : 1, kArenaAlign); }
     bool alloc(uint64_t bytes, uint64_t* off) {
         const uint64_t b = span(bytes);
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < b) continue;
-            const uint64_t o = it->first, rest = it->second - b;
-            free_.erase(it);
-            if (rest) free_[o + b] = rest;
-            *off = o;
-            used_ += b;
-            peak_ = std::max(peak_, used_);
-            return true;
-        }
-        return false;
+        auto it = by_size_.lower_bound(b);
+        if (it == by_size_.end()) return false;
+        const uint64_t o = it->second, len = it->first;
+        erase_(o, len);
+        if (len > b) insert_(o + b, len - b);
+        *off = o;
+        used_ += b;
+        peak_ = std::max(peak_, used_);
+        return true;
     }
     void release(uint64_t off, uint64_t bytes) {
         const uint64_t b = span(bytes);
         used_ -= b;
         uint64_t start = off, len = b;
-        auto next = free_.lower_bound(off);
-        if (next != free_.begin()) {
+        auto next = by_off_.lower_bound(off);
+        if (next != by_off_.begin()) {
             auto prev = std::prev(next);
             if (prev->first + prev->second == off) {
                 start = prev->first;
                 len += prev->second;
-                free_.erase(prev);
+                erase_(prev->first, prev->second);
             }
         }
-        if (next != free_.end() && off + b == next->first) {
+        next = by_off_.lower_bound(off);
+        if (next != by_off_.end() && off + b == next->first) {
             len += next->second;
-            free_.erase(next);
+            erase_(next->first, next->second);
         }
-        free_[start] = len;
+        insert_(start, len);
     }
     uint64_t size() const { return size_; }
     uint64_t used() const { return used_; }
     uint64_t peak() const { return peak_; }
+    size_t holes() const { return by_off_.size(); }
 
 private:
-    std::map<uint64_t, uint64_t> free_;
+    void insert_(uint64_t off, uint64_t len) {
+        by_off_[off] = len;
+        by_size_.emplace(len, off);
+    }
+    void erase_(uint64_t off, uint64_t len) {
+        by_off_.erase(off);
+        auto range = by_size_.equal_range(len);
+        for (auto it = range.first; it != range.second; ++it)
+            if (it->second == off) {
+                by_size_.erase(it);
+                break;
+            }
+    }
+    std::map<uint64_t, uint64_t> by_off_;
+    std::multimap<uint64_t, uint64_t> by_size_;
     uint64_t size_ = 0, used_ = 0, peak_ = 0;
 };
 
@@ -105,6 +122,7 @@ struct Request {
     std::vector<AetherServeOperand> ops;
     std::vector<uint64_t> op_bytes;   // bytes of each operand's planes
     std::vector<uint64_t> op_off;     // arena offsets once admitted
+    std::vector<char> op_direct;      // host bytes the SMs can read in place (mapped pinned memory)
     std::vector<double> sc;
     std::vector<uint64_t> keys;
     void* host_out = nullptr;
@@ -121,20 +139,33 @@ struct Request {
 struct Upload {
     const void* host;
     uint64_t off, bytes;
+    bool direct;
 };
 
 struct Slot {
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr, copied = nullptr;
+    cudaEvent_t done = nullptr, copied = nullptr, done_first = nullptr;
     AgItemHost* staging = nullptr;
     void* dev_items = nullptr;
     std::vector<Request*> rs;         // the slot's requests (stable: the request deque only grows)
+    // When some requests read only resident operands and others wait for
+    // copies, the first n_first of rs run in a launch of their own that does
+    // not wait, and finish (done_first) before the rest.
+    size_t n_first = 0;
+    bool first_retired = false;
     uint64_t upload_seq = 0;
     bool busy = false;
 };
 
+// A completion seen by the loop: part 1 = the slot's first group, 2 = all.
+struct Fin {
+    Slot* s;
+    cudaError_t e;
+    int part;
+};
+
 struct Server {
-    int dev = 0;
+    int dev = 0, sms = 1;
     AetherServeConfig cfg{};
     std::vector<PlanObj*> plans;
     BatchObj* batch = nullptr;
@@ -255,7 +286,7 @@ struct Server {
             resident_bytes += R.bytes;
             created.push_back(o.id);
             refd.push_back(o.id);
-            ups.push_back(Upload{o.host, off, R.bytes});
+            ups.push_back(Upload{o.host, off, R.bytes, cfg.upload_engine == 0 && r.op_direct[i] != 0});
             r.uploaded += R.bytes;
             r.op_off[i] = off;
             ++st.resident_misses;
@@ -281,18 +312,49 @@ struct Server {
 
     // Enqueue the copies, the launch and the output copies of one slot (mu not held).
     void enqueue(Slot& S, const std::vector<Upload>& ups, bool wait_uploads) {
-        for (const Upload& u : ups)
-            ag_ck(cudaMemcpyAsync(base + u.off, u.host, u.bytes, cudaMemcpyHostToDevice, copy_stream),
-                  "cudaMemcpyAsync(operand)");
+        // Mapped pinned sources go through one gather kernel per slot (in
+        // launches of up to kAgCopyMaxSegments); the rest through the copy engine.
+        AgCopyBatch gb;
+        gb.n = 0;
+        for (const Upload& u : ups) {
+            if (!u.direct) {
+                ag_ck(cudaMemcpyAsync(base + u.off, u.host, u.bytes, cudaMemcpyHostToDevice, copy_stream),
+                      "cudaMemcpyAsync(operand)");
+                continue;
+            }
+            gb.seg[gb.n++] = AgCopySegment{u.host, base + u.off, u.bytes};
+            if (gb.n == kAgCopyMaxSegments) {
+                ag_ck(ag_gather_copy(gb, sms, copy_stream), "gather copy");
+                gb.n = 0;
+            }
+        }
+        if (gb.n) ag_ck(ag_gather_copy(gb, sms, copy_stream), "gather copy");
         if (!ups.empty() || wait_uploads) {
             ag_ck(cudaEventRecord(S.copied, copy_stream), "cudaEventRecord(copied)");
             ag_ck(cudaStreamWaitEvent(S.stream, S.copied, 0), "cudaStreamWaitEvent(copied)");
         }
+        const bool need_wait = !ups.empty() || wait_uploads;
+        if (!need_wait) S.n_first = 0;
+        if (S.n_first) {
+            launch_group(S, 0, S.n_first);
+            ag_ck(cudaEventRecord(S.done_first, S.stream), "cudaEventRecord(done_first)");
+        }
+        if (need_wait) {
+            ag_ck(cudaEventRecord(S.copied, copy_stream), "cudaEventRecord(copied)");
+            ag_ck(cudaStreamWaitEvent(S.stream, S.copied, 0), "cudaStreamWaitEvent(copied)");
+        }
+        launch_group(S, S.n_first, S.rs.size() - S.n_first);
+        ag_ck(cudaEventRecord(S.done, S.stream), "cudaEventRecord(done)");
+    }
+
+    // Launch requests [first, first + count) of a slot on its stream, then
+    // their host output copies. One request runs its plan's own kernel (no
+    // work list, same arithmetic); several run as one batched kernel.
+    void launch_group(Slot& S, size_t first, size_t count) {
+        if (!count) return;
         std::vector<AetherOperand> ops;
-        // A launch of one request needs no work list: its plan's own kernel
-        // runs it with the same arithmetic and one copy fewer.
-        if (cfg.mode == AETHER_SERVE_PLAIN || S.rs.size() == 1) {
-            const Request& r = *S.rs[0];
+        if (count == 1) {
+            const Request& r = *S.rs[first];
             PlanObj* P = plans[size_t(r.plan)];
             AetherLaunch a = launch_of(r, ops);
             AgArgsHost k;
@@ -307,9 +369,9 @@ struct Server {
                   "cudaLaunchKernel(plain)");
         } else {
             uint64_t tiles = 0;
-            for (size_t i = 0; i < S.rs.size(); ++i) {
-                const Request& r = *S.rs[i];
-                AgItemHost& h = S.staging[i];
+            for (size_t i = 0; i < count; ++i) {
+                const Request& r = *S.rs[first + i];
+                AgItemHost& h = S.staging[first + i];
                 h = AgItemHost{};
                 AetherLaunch a = launch_of(r, ops);
                 make_args(batch->plans[size_t(r.plan)], &a, h.a);   // alignment was checked at submit
@@ -318,53 +380,62 @@ struct Server {
                 const uint64_t per = batch_tile_samples(*batch, r.plan);
                 tiles += (r.n + per - 1) / per;
             }
-            const int n_items = int(S.rs.size());
-            ag_ck(cudaMemcpyAsync(S.dev_items, S.staging, size_t(n_items) * sizeof(AgItemHost), cudaMemcpyHostToDevice,
-                                  S.stream),
+            AgItemHost* dev = static_cast<AgItemHost*>(S.dev_items) + first;
+            ag_ck(cudaMemcpyAsync(dev, S.staging + first, count * sizeof(AgItemHost), cudaMemcpyHostToDevice, S.stream),
                   "cudaMemcpyAsync(work list)");
-            void* items = S.dev_items;
-            int n = n_items;
+            void* items = dev;
+            int n = int(count);
             uint64_t t = tiles;
             void* params[] = {&items, &n, &t};
             ag_ck(cudaLaunchKernel(reinterpret_cast<const void*>(batch->kernel), dim3(batch_grid(*batch, tiles)),
                                    dim3(unsigned(batch->block)), params, 0, S.stream),
                   "cudaLaunchKernel(batch)");
         }
-        for (const Request* rp : S.rs) {
-            const Request& r = *rp;
+        for (size_t i = 0; i < count; ++i) {
+            const Request& r = *S.rs[first + i];
             if (r.host_out)
                 ag_ck(cudaMemcpyAsync(r.host_out, base + r.out_off, r.out_bytes, cudaMemcpyDeviceToHost, S.stream),
                       "cudaMemcpyAsync(output)");
         }
-        ag_ck(cudaEventRecord(S.done, S.stream), "cudaEventRecord(done)");
     }
 
-    // Retire the slots whose completion events fired (mu held).
-    void retire(const std::vector<std::pair<Slot*, cudaError_t>>& fin, uint64_t t) {
-        for (const auto& f : fin) {
-            Slot& S = *f.first;
-            const cudaError_t e = f.second;
-            if (e != cudaSuccess && fatal.empty()) fatal = std::string("serve: launch failed: ") + cudaGetErrorString(e);
-            for (Request* rp : S.rs) {
-                Request& r = *rp;
-                for (const AetherServeOperand& o : r.ops) unref(o.id);
-                if (e != cudaSuccess) {
-                    fail_request(r, fatal);
-                } else {
-                    r.state = AETHER_SERVE_DONE;
-                    r.t_done = t;
-                    ++st.completed;
-                    st.bytes += r.bytes;
-                    st.uploaded_bytes += r.uploaded;
-                    st.last_done_ns = std::max(st.last_done_ns, t);
-                }
-                if (!(r.flags & AETHER_SERVE_KEEP_OUTPUT) || e != cudaSuccess) {
-                    arena.release(r.out_off, r.out_bytes);
-                    r.out_live = false;
-                }
+    // Retire requests [b, e) of a slot that finished with status `err` (mu held).
+    void retire_range(Slot& S, size_t b, size_t e, cudaError_t err, uint64_t t) {
+        if (err != cudaSuccess && fatal.empty()) fatal = std::string("serve: launch failed: ") + cudaGetErrorString(err);
+        for (size_t i = b; i < e; ++i) {
+            Request& r = *S.rs[i];
+            for (const AetherServeOperand& o : r.ops) unref(o.id);
+            if (err != cudaSuccess) {
+                fail_request(r, fatal);
+            } else {
+                r.state = AETHER_SERVE_DONE;
+                r.t_done = t;
+                ++st.completed;
+                st.bytes += r.bytes;
+                st.uploaded_bytes += r.uploaded;
+                st.last_done_ns = std::max(st.last_done_ns, t);
             }
+            if (!(r.flags & AETHER_SERVE_KEEP_OUTPUT) || err != cudaSuccess) {
+                arena.release(r.out_off, r.out_bytes);
+                r.out_live = false;
+            }
+        }
+    }
+
+    // Retire what the completion events say finished (mu held).
+    void retire(const std::vector<Fin>& fin, uint64_t t) {
+        for (const Fin& f : fin) {
+            Slot& S = *f.s;
+            if (f.part == 1) {
+                retire_range(S, 0, S.n_first, f.e, t);
+                S.first_retired = true;
+                continue;
+            }
+            retire_range(S, S.first_retired ? S.n_first : 0, S.rs.size(), f.e, t);
             uploads_done_seq = std::max(uploads_done_seq, S.upload_seq);
             S.rs.clear();
+            S.n_first = 0;
+            S.first_retired = false;
             S.busy = false;
         }
         if (!fin.empty()) cv_done.notify_all();
@@ -397,7 +468,7 @@ struct Server {
     void run() {
         cudaSetDevice(dev);
         const size_t limit = cfg.mode == AETHER_SERVE_PLAIN ? 1 : size_t(cfg.max_items);
-        std::vector<std::pair<Slot*, cudaError_t>> fin;
+        std::vector<Fin> fin;
         std::unique_lock<std::mutex> lk(mu, std::defer_lock);
         const uint64_t spin_ns = uint64_t(cfg.idle_spin_us) * 1000u;
         uint64_t last_work = now();
@@ -405,10 +476,19 @@ struct Server {
             fin.clear();
             for (Slot& S : slots) {
                 if (!S.busy) continue;
+                if (S.n_first && !S.first_retired) {
+                    const cudaError_t e1 = cudaEventQuery(S.done_first);
+                    if (e1 != cudaErrorNotReady) {
+                        if (e1 != cudaSuccess) cudaGetLastError();
+                        fin.push_back(Fin{&S, e1, 1});
+                    }
+                }
                 const cudaError_t e = cudaEventQuery(S.done);
                 if (e == cudaErrorNotReady) continue;
                 if (e != cudaSuccess) cudaGetLastError();
-                fin.emplace_back(&S, e);
+                if (S.n_first && !S.first_retired && (fin.empty() || fin.back().s != &S))
+                    fin.push_back(Fin{&S, e, 1});   // the first group finished before the rest
+                fin.push_back(Fin{&S, e, 2});
             }
             const uint64_t t_fin = fin.empty() ? 0 : now();
             lk.lock();
@@ -423,8 +503,17 @@ struct Server {
             if (S && !queue.empty() && fatal.empty()) {
                 std::vector<Upload> ups;
                 bool wait_uploads = false;
+                const uint64_t ta = now();
                 blocked = admit(*S, limit, ups, wait_uploads);
+                st.admit_ns += now() - ta;
                 if (!S->rs.empty()) {
+                    // requests that read resident operands only go first
+                    auto mid = std::stable_partition(S->rs.begin(), S->rs.end(), [](const Request* r) {
+                        return r->uploaded == 0 && !r->wait_upload;
+                    });
+                    const size_t ready = size_t(mid - S->rs.begin());
+                    S->n_first = (ready > 0 && ready < S->rs.size()) ? ready : 0;
+                    S->first_retired = false;
                     S->busy = true;
                     // The completion of a slot that waited for the copy stream
                     // proves every copy enqueued before its wait has landed.
@@ -462,6 +551,8 @@ struct Server {
                             fail_request(r, err);
                         }
                         S->rs.clear();
+                        S->n_first = 0;
+                        S->first_retired = false;
                         S->busy = false;
                         cv_done.notify_all();
                     }
@@ -495,6 +586,22 @@ struct Server {
 };
 
 uint64_t planes_of(ag::DType d, int comps) { return uint64_t(comps) * (d == ag::DType::FF ? 2u : 1u); }
+
+// Whether [p, p + bytes) is pinned host memory the device reads at the same
+// address (16-byte aligned at the start): checked at both ends.
+bool mapped_host(const void* p, uint64_t bytes) {
+    if (!bytes || (reinterpret_cast<uintptr_t>(p) & 15u)) return false;
+    const char* ends[2] = {static_cast<const char*>(p), static_cast<const char*>(p) + bytes - 1};
+    for (const char* q : ends) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (at.type != cudaMemoryTypeHost || at.devicePointer != q) return false;
+    }
+    return true;
+}
 
 int serve_fail(const std::string& m) { return ag_internal_fail(m.c_str()); }
 
@@ -542,6 +649,7 @@ Request build_request(Server* S, const AetherServeRequest* q) {
         const uint64_t b = planes_of(pl.operand_dtype[i], comps) * o.pitch * uint64_t(es);
         r.ops.push_back(o);
         r.op_bytes.push_back(b);
+        r.op_direct.push_back(o.host && mapped_host(o.host, b) ? 1 : 0);
         need += Arena::span(b);
         r.bytes += q->n * planes_of(pl.operand_dtype[i], comps) * uint64_t(es);
     }
@@ -602,6 +710,7 @@ void destroy(Server* S) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.copied) cudaEventDestroy(sl.copied);
+        if (sl.done_first) cudaEventDestroy(sl.done_first);
         if (sl.staging) cudaFreeHost(sl.staging);
         if (sl.dev_items) cudaFree(sl.dev_items);
         if (sl.stream) cudaStreamDestroy(sl.stream);
@@ -643,6 +752,7 @@ AG_EXPORT int aether_serve_open(void* const* plans, int n_plans, const AetherSer
             S->plans.push_back(P);
         }
         ag_ck(cudaGetDevice(&S->dev), "cudaGetDevice");
+        ag_ck(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->dev), "cudaDeviceGetAttribute");
         AetherLowering low{};
         low.block = S->cfg.block;
         low.ipt = S->cfg.ipt;
@@ -661,6 +771,7 @@ AG_EXPORT int aether_serve_open(void* const* plans, int n_plans, const AetherSer
             ag_ck(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking), "cudaStreamCreate(slot)");
             ag_ck(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming), "cudaEventCreate");
             ag_ck(cudaEventCreateWithFlags(&sl.copied, cudaEventDisableTiming), "cudaEventCreate");
+            ag_ck(cudaEventCreateWithFlags(&sl.done_first, cudaEventDisableTiming), "cudaEventCreate");
             void* h = nullptr;
             ag_ck(cudaMallocHost(&h, items * sizeof(AgItemHost)), "cudaMallocHost(work list)");
             sl.staging = static_cast<AgItemHost*>(h);

@@ -324,6 +324,7 @@ def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, satu
                "resident_hit_rate": round(st["resident_hits"] / max(1, st["resident_hits"] + st["resident_misses"]), 3),
                "uploaded_gb": round(st["uploaded_bytes"] / 1e9, 2), "evictions": st["evictions"],
                "enqueue_us_per_launch": round(st["enqueue_ns"] / 1e3 / max(1, st["launches"]), 2),
+               "admit_us_per_launch": round(st["admit_ns"] / 1e3 / max(1, st["launches"]), 2),
                "arena_peak_gb": round(st["arena_peak_bytes"] / 1e9, 1), "failed": st["failed"]}
         out.update(serve.latency_summary(sts[len(sts) // 10:]))
         return out

@@ -216,7 +216,8 @@ typedef struct AetherServeConfig {
     int max_items;             /* requests per batched launch; 0 = 256 */
     int block, ipt;            /* lowering of the batched kernel; 0 = 512, 1 */
     int idle_spin_us;          /* the loop polls this long after its last work before it sleeps; 0 = 2000 */
-    int reserved;
+    int upload_engine;         /* 0: SMs read mapped pinned host operands in one gather kernel per launch
+                                  (other memory: copy engine); 1: copy engine only */
 } AetherServeConfig;
 
 typedef struct AetherServeOperand {
@@ -258,6 +259,7 @@ typedef struct AetherServeStats {
     uint64_t arena_bytes, arena_peak_bytes, resident_bytes;
     uint64_t first_arrival_ns, last_done_ns;
     uint64_t enqueue_ns;      /* host time the loop spent issuing copies and launches */
+    uint64_t admit_ns;        /* host time the loop spent admitting (arena, residency) */
 } AetherServeStats;
 
 /* Compile the batched kernel for `plans` (none may be a sum plan), allocate the

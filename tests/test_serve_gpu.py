@@ -95,6 +95,10 @@ def test_same_alone_in_mix_and_plain(shapes, pools):
     assert pstats["launches"] == len(trace)
     for a, p in zip(alone, plain):
         assert torch.equal(a, p)
+    # operands through the copy engine instead of the SM gather kernel
+    copied, _, _ = _mixed(shapes, pools, trace, max_items=64, upload_engine="copy")
+    for a, c in zip(alone, copied):
+        assert torch.equal(a, c)
     assert stats["resident_hits"] > 0 and stats["completed"] == len(trace)
 
 
@@ -149,6 +153,18 @@ def test_refusals_and_kept_outputs(shapes, pools):
         bad = srv.request(cross, 2000, [7, 9], [pools.window("f64", 7, 3 * 2016 * 8), pools.window("f64", 9, 3 * 2016 * 8)])
         with pytest.raises(ag.AetherError, match="resident with"):
             srv.wait(srv.submit(bad))
+        # pageable host bytes take the copy engine
+        pa, pb = (np.ascontiguousarray(pools.array("f64", i, 3, 1024)) for i in (31, 32))
+        pg = srv.request(cross, 1000, [31, 32], [pa.ctypes.data, pb.ctypes.data], keep=True)
+        tp = srv.submit(pg)
+        stp = srv.wait(tp)
+        host2 = torch.zeros(3 * 1024, dtype=torch.float64, pin_memory=True)
+        _abi.check(_abi.lib().aether_copy(2, 0, ctypes.c_void_p(host2.data_ptr()), 1, 0, ctypes.c_void_p(stp["output"]),
+                                          host2.numel() * 8, None))
+        _abi.check(_abi.lib().aether_stream_sync(0, None))
+        np.testing.assert_allclose(host2.numpy().reshape(3, -1)[:, :1000], np.cross(pa[:, :1000].T, pb[:, :1000].T).T,
+                                   rtol=0, atol=EMU_ATOL)
+        srv.release(tp)
         # an id that is resident needs no host bytes
         again = srv.request(cross, 1000, [7, 8], [0, 0])
         assert srv.wait(srv.submit(again))["uploaded_bytes"] == 0
