@@ -396,6 +396,9 @@ bool make_args(const PlanObj* P, const AetherLaunch* a, AgArgsHost& k) {
         aligned = aligned && (reinterpret_cast<uintptr_t>(o.ptr) % 16 == 0) && (comps == 1 || (pitch * es) % 16 == 0);
     }
     for (int i = 0; i < pl.n_scalars; ++i) {
+        if (size_t(i) < pl.scalar_nonneg.size() && pl.scalar_nonneg[size_t(i)] && !(a->scalars[i] >= 0.0))
+            throw std::runtime_error("plan_launch: scalar " + std::to_string(i) +
+                                     " must be >= 0 (the plan was generated for a non-negative value)");
         k.sc[i] = a->scalars[i];
         k.sch[i] = float(a->scalars[i]);
         k.scl[i] = std::isfinite(k.sch[i]) ? float(a->scalars[i] - double(k.sch[i])) : 0.0f;

@@ -105,6 +105,19 @@ __device__ __forceinline__ df sqr(df x) {
 }
 // Scale by an exact power of two.
 __device__ __forceinline__ df scale(df x, float p2) { return mk(__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)); }
+// Sum where the first term dominates: |x.hi| >= |y.hi| (or x == 0), so the
+// leading sum is exact by Fast2Sum (Dekker 1971) without the six-operation
+// two-sum; the error is that of add_fast. Used where the caller's argument
+// ranges prove the ordering.
+__device__ __forceinline__ df add_quick(df x, df y) {
+    const df s = fast_two_sum(x.hi, y.hi);
+    const float v = __fadd_rn(__fadd_rn(x.lo, y.lo), s.lo);
+    return fast_two_sum(s.hi, v);
+}
+__device__ __forceinline__ df add_quick(df x, float y) {
+    const df s = fast_two_sum(x.hi, y);
+    return fast_two_sum(s.hi, __fadd_rn(x.lo, s.lo));
+}
 
 // Hardware seeds (MUFU). The host branch exists only so the double-float
 // algorithms can be checked by a host build of this header.
@@ -243,12 +256,13 @@ __device__ __forceinline__ df exp_(df x) {
     const float rh = r.hi;
     const float tail = __fmul_rn(__fmul_rn(rh, __fmul_rn(rh, rh)),
                                  __fmaf_rn(rh, __fmaf_rn(rh, 8.33333333e-3f, 4.16666667e-2f), 1.66666667e-1f));
-    df p = add_fast(r, scale(sqr(r), 0.5f));
-    p = add(p, tail);
+    // |r| <= ln2/128, so each sum below is led by its first term
+    df p = add_quick(r, scale(sqr(r), 0.5f));
+    p = add_quick(p, tail);
     const int j = m & 63;
     int k = m >> 6;
     const df T = mk(__ldg(&kExp2TabHi[j]), __ldg(&kExp2TabLo[j]));
-    const df res = add_fast(T, mul(T, p));
+    const df res = add_quick(T, mul(T, p));
     k = k < -126 ? -126 : (k > 126 ? 126 : k);
     return scale(res, p2f(k));
 }
@@ -265,8 +279,8 @@ __device__ __forceinline__ df log1p_poly(df t) {
     const df t2 = sqr(t);
     const float th = t.hi;
     const float q = __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, 0.2f, -0.25f), 0.333333333f));
-    const df s = add_fast(t, scale(t2, -0.5f));
-    return add(s, __fmul_rn(t2.hi, q));
+    const df s = add_quick(t, scale(t2, -0.5f));
+    return add_quick(s, __fmul_rn(t2.hi, q));
 }
 __device__ __forceinline__ df log_s(float s, df x) {
     const float yh = __fadd_rn(s, x.hi);
@@ -286,12 +300,12 @@ __device__ __forceinline__ df log_s(float s, df x) {
     const df t = add(B, C);
     const df lp = log1p_poly(t);
     const df L = mk(__ldg(&kLogLHi[i]), __ldg(&kLogLLo[i]));
-    const float fe = (float)e;
-    const df p2 = two_prod(fe, AG_LN2_2);
-    const df E = add(fast_two_sum(__fmul_rn(fe, AG_LN2_1), p2.hi), __fmaf_rn(fe, AG_LN2_3, p2.lo));
-    // |lp| < |L| except for i == 0 (L = 0), and e ln2 + L cancels by at most a
-    // factor 2.4, so the sums need no cancellation-safe form.
-    const df res = add_fast(E, add_fast(L, lp));
+    // e ln2 from a table (the index is clamped; out-of-range e is flagged below)
+    const int ei = (e < -127 ? -127 : (e > 128 ? 128 : e)) + AG_LN2_TAB_OFF;
+    const df E = mk(__ldg(&kLn2MulHi[ei]), __ldg(&kLn2MulLo[ei]));
+    // |lp| <= 2^-10.6 <= |L| except for i == 0 (L = 0), and |E| >= ln2 >
+    // |L + lp| except for e == 0 (E = 0): each sum is led by its first term.
+    const df res = add_quick(E, add_quick(L, lp));
     const bool valid = yh > 0.0f && e > -120 && e < 120;
     return valid ? res : mk(__int_as_float(0x7fc00000), 0.0f);
 }
@@ -315,18 +329,20 @@ __device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
     const float th2 = __fmul_rn(th, th);
     // sin t = t - t^3/6 + t^5/120
     const df t3 = mul(t2, t);
-    const df st = add_fast(t, add(mul(t3, mk(-AG_SIXTH_HI, -AG_SIXTH_LO)),
-                                  __fmul_rn(__fmul_rn(t3.hi, th2), 8.33333333e-3f)));
+    const df st = add_quick(t, add_quick(mul(t3, mk(-AG_SIXTH_HI, -AG_SIXTH_LO)),
+                                         __fmul_rn(__fmul_rn(t3.hi, th2), 8.33333333e-3f)));
     // cos t - 1 = -t^2/2 + t^4/24 - t^6/720
     const float c4 = __fmul_rn(__fmul_rn(th2, th2), __fmaf_rn(th2, -1.38888889e-3f, 4.16666667e-2f));
-    const df cm1 = add(scale(t2, -0.5f), c4);
+    const df cm1 = add_quick(scale(t2, -0.5f), c4);
     const int qq = (q + (want_cos ? 1 : 0)) & 3;   // cos x = sin(x + pi/2)
     const bool odd = qq & 1;
     const df S = mk(__ldg(&kSinTabHi[j]), __ldg(&kSinTabLo[j]));
     const df C = mk(__ldg(&kCosTabHi[j]), __ldg(&kCosTabLo[j]));
     const df A = odd ? C : S;
     const df B = odd ? neg(S) : C;
-    const df v = add(add(A, mul(A, cm1)), mul(B, st));
+    // |A (1 + cm1)| >= 2 |B st| (or A = 0 at j = 0): |S_j| >= sin(1/32) for
+    // j != 0 while |st| <= sin(1/64)
+    const df v = add_quick(add_quick(A, mul(A, cm1)), mul(B, st));
     return (qq & 2) ? neg(v) : v;
 }
 // Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.

@@ -91,6 +91,11 @@ def main():
     l1 = trunc_bits(ln2, 16)
     l2 = trunc_bits(ln2 - l1, 24)
     l3 = f32(ln2 - l1 - l2)
+    # e ln2 for e in [-127, 128] as a float pair (the exponent part of a log)
+    e_hi, e_lo = zip(*[split2(e * ln2) for e in range(-127, 129)])
+    out.append("#define AG_LN2_TAB_OFF 127")
+    out.append("__device__ const float kLn2MulHi[256] = {%s};" % ", ".join(fl(v) for v in e_hi))
+    out.append("__device__ const float kLn2MulLo[256] = {%s};" % ", ".join(fl(v) for v in e_lo))
     out.append("#define AG_LN2_1 %s" % fl(l1))
     out.append("#define AG_LN2_2 %s" % fl(l2))
     out.append("#define AG_LN2_3 %s" % fl(l3))

@@ -175,6 +175,12 @@ struct Parser {
             n.k = integer();
             if (n.k < 0 || n.k >= 16) fail("scalar slot out of range");
             plan.n_scalars = std::max(plan.n_scalars, n.k + 1);
+            if (peek() == "+") {
+                tok();
+                n.nonneg_hint = true;
+                plan.scalar_nonneg.resize(size_t(plan.n_scalars), 0);
+                plan.scalar_nonneg[size_t(n.k)] = 1;
+            }
         } else if (op == "lit") {
             const std::string t = tok();
             char* end = nullptr;
@@ -412,6 +418,7 @@ struct Gen {
             op == "sqnorm" || op == "rnorm" || op == "exp2" || op == "cosh")
             r = true;
         else if (op == "lit") r = n.lit >= 0.0;
+        else if (op == "sc") r = n.nonneg_hint;
         else if (op == "bcast" || op == "at0") r = nonneg(n.kids[0]);
         else if (op == "mul") r = n.kids[0] == n.kids[1] || (nonneg(n.kids[0]) && nonneg(n.kids[1]));
         else if (op == "add" || op == "scale") r = nonneg(n.kids[0]) && nonneg(n.kids[1]);

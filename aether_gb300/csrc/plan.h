@@ -25,6 +25,7 @@ struct Node {
     std::vector<int> ints;    // further integer arguments
     double lit = 0.0;
     DType dtype = DType::F64; // storage type of an `in` leaf
+    bool nonneg_hint = false; // `(sc K +)`: the launch promises a value >= 0
 };
 
 struct Plan {
@@ -39,6 +40,7 @@ struct Plan {
     int n_keys = 0;
     std::vector<DType> operand_dtype;
     std::vector<int> operand_comps;
+    std::vector<char> scalar_nonneg;   // per scalar slot: launches must pass a value >= 0
     bool has_random = false;
     bool wants_sum() const { return op == "sum" || op == "setsum"; }
     bool wants_store() const { return op != "sum"; }

@@ -233,7 +233,8 @@ class Scalar(Expr):
         self.v = float(v)
 
     def ir(self, ctx):
-        return "(sc %d)" % ctx.scalar(self.v)
+        # a non-negative value is marked so the plan can drop cancellation-safe sums
+        return ("(sc %d +)" if self.v >= 0.0 else "(sc %d)") % ctx.scalar(self.v)
 
 
 class Literal(Expr):

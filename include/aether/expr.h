@@ -163,7 +163,10 @@ struct Leaf : Node {
 
 struct ScalarNode : Node {
     double v;
-    std::string text(Context& ctx) const override { return "(sc " + std::to_string(ctx.scalar(v)) + ")"; }
+    // a non-negative value is marked so the plan can drop cancellation-safe sums
+    std::string text(Context& ctx) const override {
+        return "(sc " + std::to_string(ctx.scalar(v)) + (v >= 0.0 ? " +)" : ")");
+    }
 };
 
 struct LiteralNode : Node {

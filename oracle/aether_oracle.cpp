@@ -269,6 +269,7 @@ struct Parser {
             n.shape = parse_shape(lx.tok());
         } else if (op == "sc") {
             n.k = integer();
+            if (lx.peek() == "+") lx.tok();   // sign hint: the value is >= 0
         } else if (op == "lit") {
             n.lit = std::strtod(lx.tok().c_str(), nullptr);
         } else if (op == "bcast") {
