@@ -242,7 +242,71 @@ def secondary_config3(ag, n=1 << 27):
     res["global_sum_rel_diff"] = abs((s32[0] + s32[1]) - (s64[0] + s64[1])) / abs(s64[0] + s64[1])
     res["speedup_vs_fp64"] = round(best / ms32, 3)
     res["gbs_ff"] = round(n * 68 / (ms32 * 1e-3) / 1e9, 1)
+    del x64, y64, d64, d32
+    torch.cuda.empty_cache()
+    res["p1_p2"] = config3_expressions(ag, n)
     return res
+
+
+def config3_expressions(ag, n):
+    """Config 3 P1 and P2: the plain fused expression (a up to +-1e5, so the
+    sine reduces in FP64) and the large streaming expression (log-uniform
+    magnitudes 1e-6..1e6, random sign) on Array<float,3> inputs with
+    float-float outputs, against the same FP32 values in FP64 storage; error
+    per output relative to native FP64 evaluation (CUDA's FP64 functions)."""
+    import torch
+    g = ag.Generator(31)
+
+    def loguniform(arr, k):
+        sign = g.substream(2 * k).bernoulli(3, 0.5) * 2.0 - 1.0
+        ag.assign(arr, sign * ag.cwiseExp(g.substream(2 * k + 1).uniform(3, -6.0, 6.0) * 2.302585092994046))
+
+    def p1(v):
+        a, b, c = v
+        return a + b * c + ag.cwiseSin(a) * ag.cwiseExp((c * c) * (-1.0))
+
+    def p2(v):
+        a, b, c, d0 = v
+        return ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c)) + \
+            ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0)
+
+    out = {}
+    for name, fn, k_in, fill, bff, b64 in (("p1", p1, 3, "p1", 60, 96), ("p2", p2, 4, "log", 72, 120)):
+        ins = [ag.Array("f32", (3,), n) for _ in range(k_in)]
+        for k, x in enumerate(ins):
+            if fill == "p1":
+                lo, hi = (-1e5, 1e5) if k == 0 else (-1.0, 1.0)
+                ag.assign(x, g.substream(40 + k).uniform(3, lo, hi))
+            else:
+                loguniform(x, 10 + k)
+        dff = ag.Array("ff", (3,), n)
+        Lff = ag.prepare(dff, fn([x.view() for x in ins]), math=2)
+        ms_ff = _time_ms(Lff)
+        ins64 = []
+        for x in ins:
+            y = ag.Array("f64", (3,), n)
+            y.data.copy_(x.data)
+            ins64.append(y)
+        del ins
+        d64 = ag.Array("f64", (3,), n)
+        best = None
+        for m in (0, 1):
+            L64 = ag.prepare(d64, fn([x.view() for x in ins64]), math=m)
+            ms = _time_ms(L64)
+            best = ms if best is None else min(best, ms)
+        ag.prepare(d64, fn([x.view() for x in ins64]), math=0)()   # FP64 reference values
+        torch.cuda.synchronize()
+        v = dff.data[:3, :n].double() + dff.data[3:, :n].double()
+        ref = d64.data[:, :n]
+        rel = torch.abs(v - ref) / torch.clamp(torch.abs(ref), min=1e-300)
+        finite = torch.isfinite(ref)
+        out[name] = {"ff_ms": round(ms_ff, 4), "f64_ms": round(best, 4), "speedup_vs_fp64": round(best / ms_ff, 3),
+                     "ff_samples_per_s": round(n / (ms_ff * 1e-3), 1), "bytes_per_sample_ff": bff,
+                     "bytes_per_sample_f64": b64, "max_rel_err_vs_fp64": float(torch.max(rel[finite]).item()),
+                     "median_rel_err_vs_fp64": float(torch.median(rel[finite]).item())}
+        del ins64, d64, dff
+        torch.cuda.empty_cache()
+    return out
 
 
 def config4_workload(ag, n_items=4096, median=4096, sigma=1.5, lo=64, hi=1 << 21, seed=4, math=1):
