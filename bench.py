@@ -10,7 +10,8 @@ value = algorithmic bytes of both kernels / device time (inputs resident in
 HBM, CUDA events on the launching stream). Inputs are larger than L2, so no
 flush runs between steps. e2e = the same step through the C-ABI with pinned
 host buffers: host->device copies of the four inputs and device->host copies
-of both outputs inside the timed region.
+of both outputs inside the timed region, pipelined over sample blocks
+(partition_view) on three streams so uploads, kernels and downloads overlap.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -475,19 +476,48 @@ def run_ours(args):
             h.copy_(x.data[:, :N_EXPR])
         host_out = torch.empty((3, N_EXPR), dtype=torch.float64, pin_memory=True)
         host_fill = torch.empty((1, N_FILL), dtype=torch.float64, pin_memory=True)
-        s = ctypes.c_void_p(stream.cuda_stream)
+        # The step cut into K sample blocks (partition_view), each block's
+        # uploads, kernels and downloads on one of three streams, so block
+        # r+1 copies in while block r computes and block r-1 copies out.
+        K = max(1, args.e2e_chunks)
+        streams = [torch.cuda.Stream() for _ in range(3)]
+        pitch_e = ag.padded_block_samples(N_EXPR, K)
+        pitch_f = ag.padded_block_samples(N_FILL, K)
+        chunks = []
+        for r in range(K):
+            bi = [ag.partition_view(x, K, r) for x in arrs]
+            bo = ag.partition_view(d, K, r)
+            bz = ag.partition_view(z, K, r)
+            if bo.n == 0 and bz.n == 0:
+                continue
+            a_, b_, c_, d0_ = (x.view() for x in bi)
+            e_r = ag.cwiseSqrt(a_ * a_ + b_ * b_) * ag.cwiseLog1p(ag.cwiseAbs(c_)) + \
+                ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0_ * d0_)
+            ke = ag.prepare(bo, e_r, math=math_mode, tune=not args.no_tune) if bo.n else None
+            kf = ag.prepare(bz, g.substream(4).normal(1, 0.0, 1.0), sample_offset=r * pitch_f, math=math_mode,
+                            tune=not args.no_tune) if bz.n else None
+            chunks.append((r * pitch_e, bo.n, r * pitch_f, bz.n, ke, kf))
+        cap = arrs[0].capacity
 
         def e2e_step():
-            for h, x in zip(host_in, arrs):
-                ag._abi.check(L.aether_copy(1, local, ctypes.c_void_p(x.data.data_ptr()), 2, 0,
-                                            ctypes.c_void_p(h.data_ptr()), nb, s))
-            k_expr()
-            k_fill()
-            ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_out.data_ptr()), 1, local,
-                                        ctypes.c_void_p(d.data.data_ptr()), nb, s))
-            ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_fill.data_ptr()), 1, local,
-                                        ctypes.c_void_p(z.data.data_ptr()), N_FILL * 8, s))
-            ag._abi.check(L.aether_stream_sync(local, s))
+            for k, (e0, en, f0, fn, ke, kf) in enumerate(chunks):
+                st = streams[k % len(streams)]
+                sp = ctypes.c_void_p(st.cuda_stream)
+                for h, x in zip(host_in, arrs):
+                    for c in range(3):
+                        ag._abi.check(L.aether_copy(1, local, ctypes.c_void_p(x.data.data_ptr() + (c * cap + e0) * 8), 2, 0,
+                                                    ctypes.c_void_p(h.data_ptr() + (c * N_EXPR + e0) * 8), en * 8, sp))
+                if ke is not None:
+                    ke(st.cuda_stream)
+                if kf is not None:
+                    kf(st.cuda_stream)
+                for c in range(3):
+                    ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_out.data_ptr() + (c * N_EXPR + e0) * 8), 1,
+                                                local, ctypes.c_void_p(d.data.data_ptr() + (c * cap + e0) * 8), en * 8, sp))
+                ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_fill.data_ptr() + f0 * 8), 1, local,
+                                            ctypes.c_void_p(z.data.data_ptr() + f0 * 8), fn * 8, sp))
+            for st in streams:
+                ag._abi.check(L.aether_stream_sync(local, ctypes.c_void_p(st.cuda_stream)))
 
         e2e_step()
         torch.cuda.synchronize()
@@ -503,7 +533,8 @@ def run_ours(args):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e_ms = float(t.item())
         e2e = {"value": round(ws * (BYTES_EXPR + BYTES_FILL) / (e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
-               "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3)}
+               "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3),
+               "pipeline": "%d sample blocks over 3 streams" % len(chunks)}
 
     if rank != 0:
         if dist:
@@ -565,7 +596,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default lowering instead of the autotuned one")
-    ap.add_argument("--no-secondary", action="store_true", help="skip configs 1, 3 and 4 after the timed region")
+    ap.add_argument("--no-secondary", action="store_true", help="skip configs 1, 3, 4 and 5 after the timed region")
+    ap.add_argument("--e2e-chunks", type=int, default=16, help="sample blocks of the pipelined end-to-end step")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
     args = ap.parse_args()
