@@ -313,36 +313,40 @@ __device__ __forceinline__ df log_(df x) { return log_s(0.0f, x); }
 __device__ __forceinline__ df log1p_(df x) { return log_s(1.0f, x); }
 
 // ---------------------------------------------------------------------------
-// sin/cos: r in [-pi/4, pi/4] split as r = j/32 + t (|t| <= 1/64);
-// sin r = S_j + S_j (cos t - 1) + C_j sin t, cos r = C_j + C_j (cos t - 1) - S_j sin t.
+// sin/cos: r in [-pi/4, pi/4] (a little beyond is fine) split as r = j/2048 + t
+// with |t| <= 2^-12; with S_j, C_j = sin, cos(j/2048) from a table,
+// sin r = S_j (1 + cm1) + C_j st and cos r = C_j (1 + cm1) - S_j st, where
+// st = sin t = t + t^3 (-1/6 + t^2/120) and cm1 = cos t - 1 = t^2 (-1/2 + t^2/24).
+// For |t| <= 2^-12 the cubic and quadratic terms are below 2^-26.6 of t and of
+// 1, so they are computed in float from t.hi; only t and the products with
+// the table values are double-float.
 // ---------------------------------------------------------------------------
 // One output of sin/cos at x = q pi/2 + r: sin x is +-sin r or +-cos r by
-// quadrant, and both are A + A (cos t - 1) + B sin t with the table pair
-// (A, B) = (S_j, C_j) for sin r and (C_j, -S_j) for cos r, so only the
-// wanted one is evaluated.
+// quadrant, and both are A (1 + cm1) + B st with the table pair (A, B) =
+// (S_j, C_j) for sin r and (C_j, -S_j) for cos r, so only the wanted one is
+// evaluated.
 __device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
-    const float jf = rint_f(__fmul_rn(r.hi, 32.0f));
-    const int j = rint_i(__fmul_rn(r.hi, 32.0f)) + 26;
-    const df t = fast_two_sum(__fsub_rn(r.hi, __fmul_rn(jf, 0.03125f)), r.lo);
-    const df t2 = sqr(t);
+    int j = rint_i(__fmul_rn(r.hi, 2048.0f));
+    j = j < -AG_SC_TAB_OFF ? -AG_SC_TAB_OFF : (j > AG_SC_TAB_OFF ? AG_SC_TAB_OFF : j);   // NaN-safe index
+    const float jf = (float)j;
+    const df t = fast_two_sum(__fsub_rn(r.hi, __fmul_rn(jf, 4.8828125e-4f)), r.lo);   // exact first difference
     const float th = t.hi;
     const float th2 = __fmul_rn(th, th);
-    // sin t = t - t^3/6 + t^5/120
-    const df t3 = mul(t2, t);
-    const df st = add_quick(t, add_quick(mul(t3, mk(-AG_SIXTH_HI, -AG_SIXTH_LO)),
-                                         __fmul_rn(__fmul_rn(t3.hi, th2), 8.33333333e-3f)));
-    // cos t - 1 = -t^2/2 + t^4/24 - t^6/720
-    const float c4 = __fmul_rn(__fmul_rn(th2, th2), __fmaf_rn(th2, -1.38888889e-3f, 4.16666667e-2f));
-    const df cm1 = add_quick(scale(t2, -0.5f), c4);
+    const float cubic = __fmul_rn(__fmul_rn(th, th2), __fmaf_rn(th2, 8.33333333e-3f, -1.66666667e-1f));
+    const float cm1 = __fmul_rn(th2, __fmaf_rn(th2, 4.16666667e-2f, -0.5f));
+#ifdef __CUDA_ARCH__
+    const float4 sc = __ldg(reinterpret_cast<const float4*>(kSinCos2048) + (j + AG_SC_TAB_OFF));
+#else
+    const float* scp = kSinCos2048 + 4 * (j + AG_SC_TAB_OFF);
+    const struct { float x, y, z, w; } sc = {scp[0], scp[1], scp[2], scp[3]};
+#endif
     const int qq = (q + (want_cos ? 1 : 0)) & 3;   // cos x = sin(x + pi/2)
     const bool odd = qq & 1;
-    const df S = mk(__ldg(&kSinTabHi[j]), __ldg(&kSinTabLo[j]));
-    const df C = mk(__ldg(&kCosTabHi[j]), __ldg(&kCosTabLo[j]));
-    const df A = odd ? C : S;
-    const df B = odd ? neg(S) : C;
-    // |A (1 + cm1)| >= 2 |B st| (or A = 0 at j = 0): |S_j| >= sin(1/32) for
-    // j != 0 while |st| <= sin(1/64)
-    const df v = add_quick(add_quick(A, mul(A, cm1)), mul(B, st));
+    const df A = odd ? mk(sc.z, sc.w) : mk(sc.x, sc.y);
+    const df B = odd ? mk(-sc.x, -sc.y) : mk(sc.z, sc.w);
+    // |A| >= sin(2^-11) >= 2 |B t| for j != 0, and A = 0 at j = 0 for sin r:
+    // the sum is led by A
+    const df v = add_quick(add_quick(A, mul(B, t)), __fmaf_rn(A.hi, cm1, __fmul_rn(B.hi, cubic)));
     return (qq & 2) ? neg(v) : v;
 }
 // Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.

@@ -106,18 +106,15 @@ def main():
     out.append("#define AG_SIXTH_HI %s" % fl(t6h))
     out.append("#define AG_SIXTH_LO %s" % fl(t6l))
 
-    # --- sin/cos at j/32, j in [-26, 26] ------------------------------------
-    sh, sl, ch, cl = [], [], [], []
-    for j in range(-26, 27):
-        a = mp.mpf(j) / 32
-        h, l = split2(mp.sin(a))
-        sh.append(h)
-        sl.append(l)
-        h, l = split2(mp.cos(a))
-        ch.append(h)
-        cl.append(l)
-    for name, vals in (("kSinTabHi", sh), ("kSinTabLo", sl), ("kCosTabHi", ch), ("kCosTabLo", cl)):
-        out.append("__device__ const float %s[53] = {%s};" % (name, ", ".join(fl(v) for v in vals)))
+    # --- sin/cos at j/2048, j in [-1664, 1664], packed (S hi, S lo, C hi, C lo) --
+    # so one 16-byte load serves a lookup; |r - j/2048| <= 2^-12 leaves the
+    # cubic and quadratic terms of the remainder exact enough in float.
+    packed = []
+    for j in range(-1664, 1665):
+        a = mp.mpf(j) / 2048
+        packed += list(split2(mp.sin(a))) + list(split2(mp.cos(a)))
+    out.append("#define AG_SC_TAB_OFF 1664")
+    out.append("__device__ __align__(16) const float kSinCos2048[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
     # pi/2 in three parts: the first with 12 bits so k*P1 is exact for |k| < 2^12.
     pio2 = mp.pi / 2
     p1 = trunc_bits(pio2, 12)

@@ -10,6 +10,7 @@
 
 #define __device__
 #define __forceinline__ inline
+#define __align__(n) alignas(n)
 
 typedef unsigned int ag_u32;
 typedef unsigned long long ag_u64;
