@@ -102,6 +102,8 @@ _SIGS = {
                                    ctypes.c_size_t, _P]),
     "aether_stream_wait": (ctypes.c_int, [ctypes.c_int, _P, _P]),
     "aether_stream_sync": (ctypes.c_int, [ctypes.c_int, _P]),
+    "aether_stream_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
+    "aether_stream_destroy": (None, [_P]),
     "aether_plan_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.POINTER(_P)]),
     "aether_plan_info": (ctypes.c_int, [_P, ctypes.POINTER(AetherPlanInfo)]),
     "aether_plan_workspace_size": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),

@@ -258,6 +258,20 @@ AG_EXPORT int aether_stream_wait(int dev, void* producer, void* consumer) {
     });
 }
 
+AG_EXPORT int aether_stream_create(int dev, void** stream) {
+    return guarded([&] {
+        if (!stream) throw std::runtime_error("stream_create: null output pointer");
+        OnDevice d(dev);
+        cudaStream_t s = nullptr;
+        ck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+        *stream = s;
+    });
+}
+
+AG_EXPORT void aether_stream_destroy(void* stream) {
+    if (stream) cudaStreamDestroy(static_cast<cudaStream_t>(stream));
+}
+
 AG_EXPORT int aether_stream_sync(int dev, void* stream) {
     return guarded([&] {
         OnDevice d(dev);

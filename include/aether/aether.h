@@ -18,6 +18,7 @@
 #pragma once
 
 #include "aether/array.h"
+#include "aether/batch.h"
 #include "aether/device_flag.h"
 #include "aether/eval.h"
 #include "aether/expr.h"

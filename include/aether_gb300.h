@@ -58,6 +58,11 @@ int aether_copy(int dst_kind, int dst_dev, void* dst, int src_kind, int src_dev,
 int aether_stream_wait(int dev, void* producer, void* consumer);
 /* dsc/src/seam.h:35 stream_sync. */
 int aether_stream_sync(int dev, void* stream);
+/* No counterpart in the seam, whose callers make cudaStream_t handles with the
+ * CUDA runtime (chunk/StreamOrdered.h:38): a non-blocking stream on `dev` for
+ * callers that include no CUDA header (graph capture needs one). */
+int aether_stream_create(int dev, void** stream);
+void aether_stream_destroy(void* stream);
 
 /* ------------------------------------------------------------------------- *
  * Plans: one fused assignment `dst <op>= expr` lowered to one sm_103a kernel.

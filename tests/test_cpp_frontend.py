@@ -137,3 +137,15 @@ def test_cpp_device_flag(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0 and "device flag ok" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_cpp_batch_and_server(tmp_path):
+    """gb300::Batch (one launch and a graph replay) and gb300::Server through
+    the C++ headers equal plain per-array assignments bit for bit."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    exe = _compile(os.path.join(REPO, "tests", "cpp", "consumer_batch.cpp"), str(tmp_path / "consumer_batch"), link=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and "batch and serve ok" in r.stdout, r.stdout + r.stderr
