@@ -352,13 +352,63 @@ __device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
 // Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.
 __device__ __forceinline__ df dfc(double x);
 
-// Arguments up to 2^19 pi/2 reduce in FP64 instead (three-part pi/2 with
-// 33-bit leading parts, exact products): the one place the double-float
-// lowering uses the FP64 pipe beyond the final reassembly. Larger arguments
-// take the native path, whose FP64 reduction is total.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ ag_u64 umulhi64(ag_u64 a, ag_u64 b) { return __umul64hi(a, b); }
+#else
+inline ag_u64 umulhi64(ag_u64 a, ag_u64 b) { return (ag_u64)(((unsigned __int128)a * b) >> 64); }
+#endif
+
+// Payne-Hanek reduction (Payne & Hanek 1983) of a float h with 6000 <= |h| <
+// 2^24, in 64-bit integer arithmetic: |h| = m 2^E with a 24-bit integer m and
+// E in [-11, 0]; |h| 2/pi = m W 2^(E-192) with W = 2/pi to 192 bits, so the
+// quadrant and 128 fraction bits come out of the three 64x64 products m W_i.
+// Returns |h| - k pi/2 (a double-float, |.| <= pi/4) and k.
+__device__ __forceinline__ df reduce_ph(float h, int& k, bool& ok) {
+    const unsigned b = (unsigned)__float_as_int(h);
+    const ag_u64 m = (ag_u64)((b & 0x7fffffu) | 0x800000u);
+    int sh = 150 - (int)((b >> 23) & 0xffu);   // -E
+    ok = ok && sh >= 0 && sh <= 11;
+    sh = sh < 0 ? 0 : (sh > 11 ? 11 : sh);
+    // m W from bit 64 up, as (a2:a1:a0)
+    const ag_u64 p2h = umulhi64(m, AG_2OPI_W2);
+    const ag_u64 p1l = m * AG_2OPI_W1, p1h = umulhi64(m, AG_2OPI_W1);
+    const ag_u64 p0l = m * AG_2OPI_W0, p0h = umulhi64(m, AG_2OPI_W0);
+    const ag_u64 a0 = p1l + p2h;
+    const ag_u64 c0 = a0 < p1l ? 1ull : 0ull;
+    ag_u64 a1 = p0l + p1h;
+    ag_u64 c1 = a1 < p0l ? 1ull : 0ull;
+    a1 += c0;
+    c1 += a1 < c0 ? 1ull : 0ull;
+    const ag_u64 a2 = p0h + c1;
+    // the binary point sits sh bits into a2: integer part, then 128 fraction bits
+    ag_u64 ip = a2 >> sh;
+    ag_u64 fh = sh ? (a2 << (64 - sh)) | (a1 >> sh) : a1;
+    ag_u64 fl = sh ? (a1 << (64 - sh)) | (a0 >> sh) : a0;
+    // to the nearest quadrant: a fraction >= 1/2 becomes negative
+    const bool up = (fh >> 63) != 0;
+    ip += up ? 1ull : 0ull;
+    if (up) {
+        fl = ~fl + 1ull;
+        fh = ~fh + (fl == 0 ? 1ull : 0ull);
+    }
+    // |fraction| = (fh:fl) 2^-128, normalised: top 48 bits as a double-float
+    const int lz = fh ? __clzll((long long)fh) : 64 + __clzll((long long)(fl | 1ull));
+    ok = ok && lz < 78;   // |r| >= 2^-78: otherwise too close to k pi/2 for the float exponent range
+    const int l = lz < 78 ? lz : 77;
+    const ag_u64 top = l < 64 ? (l ? (fh << l) | (fl >> (64 - l)) : fh) : (fl << (l - 64));
+    const float th = __fmul_rn(__uint2float_rn((ag_u32)(top >> 40)), p2f(-24 - l));
+    const float tl = __fmul_rn(__uint2float_rn((ag_u32)((top >> 16) & 0xffffffu)), p2f(-48 - l));
+    df f = fast_two_sum(th, tl);
+    f = mul(f, mk(AG_PIO2_HI, AG_PIO2_LO));
+    k = (int)(ip & 3ull);
+    return up ? neg(f) : f;
+}
+
+// |x| < 6000: Cody-Waite in float (three-part pi/2, exact products for |k| <
+// 4096); 6000 <= |x| < 2^24: Payne-Hanek in integers; beyond, flagged (the
+// native lane reduces it).
 __device__ __forceinline__ df trig_(df x, bool want_cos, bool& ok) {
     const float ax = fabsf(x.hi);
-    ok = ok && ax < 823549.0f;
     df r;
     int q;
     if (ax < 6000.0f) {
@@ -369,11 +419,22 @@ __device__ __forceinline__ df trig_(df x, bool want_cos, bool& ok) {
         r = add(r, __fmul_rn(-kf, AG_PIO2_3));
         q = rint_i(__fmul_rn(x.hi, AG_TWO_OVER_PI));
     } else {
-        const double xd = (double)x.hi + (double)x.lo;
-        const double kd = rint(xd * 0.63661977236758134);
-        const double rd = ((xd - kd * AG_PIO2_D1) - kd * AG_PIO2_D2) - kd * AG_PIO2_D3;
-        r = dfc(rd);
-        q = (int)kd;
+        int k;
+        r = reduce_ph(ax, k, ok);
+        if (x.hi < 0.0f) {
+            r = neg(r);
+            k = -k;
+        }
+        r = add(r, x.lo);   // x - k pi/2 = (hi - k pi/2) + lo
+        q = k;
+        // |lo| can reach ulp(hi)/2, up to 1/2 below 2^24: bring r back into [-pi/4, pi/4]
+        if (r.hi > 0.78539816f) {
+            r = sub(r, mk(AG_PIO2_HI, AG_PIO2_LO));
+            q += 1;
+        } else if (r.hi < -0.78539816f) {
+            r = add(r, mk(AG_PIO2_HI, AG_PIO2_LO));
+            q -= 1;
+        }
     }
     return trig_core(r, q, want_cos);
 }

@@ -113,6 +113,10 @@ def main():
     for j in range(-1664, 1665):
         a = mp.mpf(j) / 2048
         packed += list(split2(mp.sin(a))) + list(split2(mp.cos(a)))
+    # 2/pi as a 192-bit fraction, three 64-bit words (Payne-Hanek reduction)
+    T = int(mp.floor(2 / mp.pi * mp.mpf(2) ** 192))
+    for k, w in enumerate(((T >> 128) & (2 ** 64 - 1), (T >> 64) & (2 ** 64 - 1), T & (2 ** 64 - 1))):
+        out.append("#define AG_2OPI_W%d 0x%016xull" % (k, w))
     out.append("#define AG_SC_TAB_OFF 1664")
     out.append("__device__ __align__(16) const float kSinCos2048[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
     # pi/2 in three parts: the first with 12 bits so k*P1 is exact for |k| < 2^12.
@@ -138,6 +142,9 @@ def main():
         out.append("#define %s %s" % (name, float(v).hex()))
     pih, pil = split2(mp.pi)
     out.append("#define AG_PI_HI %s" % fl(pih))
+    ph2, pl2 = split2(mp.pi / 2)
+    out.append("#define AG_PIO2_HI %s" % fl(ph2))
+    out.append("#define AG_PIO2_LO %s" % fl(pl2))
     out.append("#define AG_PI_LO %s" % fl(pil))
     out += ["}  // namespace e64", "}  // namespace ag", ""]
     with open(os.path.join(HERE, "ag_emu64_tables.cuh"), "w") as f:

@@ -65,6 +65,19 @@ int main() {
         [](LD x) { return sinl(x); });
     run("cos", [&] { return 2.0 * u01(rng) - 1.0; }, [](df x, bool& ok) { return cos_(x, ok); },
         [](LD x) { return cosl(x); });
+    // large float arguments (the precision form's inputs: exact in a float),
+    // 6000 <= |x| < 2^24 (the integer Payne-Hanek range), against sinl/cosl
+    {
+        Stat s;
+        for (int i = 0; i < N; ++i) {
+            const float x = (float)((u01(rng) < 0.5 ? -1 : 1) * logu(12.6, 23.99));
+            bool ok = true;
+            const df r = (i % 2) ? sin_(mk(x, 0.0f), ok) : cos_(mk(x, 0.0f), ok);
+            if (!ok || !out_ok(r)) continue;
+            s.add(val(r), (i % 2) ? sinl((LD)x) : cosl((LD)x));
+        }
+        out.push_back({"trig_large_f32", s});
+    }
     run("sin_100", [&] { return 200.0 * u01(rng) - 100.0; }, [](df x, bool& ok) { return sin_(x, ok); },
         [](LD x) { return sinl(x); });
     run("sinpi", [&] { return 2.0 * u01(rng); }, nf(sinpi_),
