@@ -116,6 +116,47 @@ class Array:
         return self
 
 
+class AccumPlane:
+    """Per-sample compensated accumulation (accum/AccumPlane.h:43-502): a value
+    plane and a compensation plane per component. `add(expr)` evaluates
+    `plane += expr` in one kernel, the exact residual of each addition going
+    to the compensation plane; with atomic=True the additions are atomic, so
+    producers on different streams may accumulate concurrently (the
+    CompensatedAtomic policy). `delivered()` is value + compensation."""
+
+    dtype = "f64"
+
+    def __init__(self, shape, n, device="cuda"):
+        self.shape = (shape,) if isinstance(shape, int) else tuple(shape)
+        self.comps = 1
+        for e in self.shape:
+            self.comps *= e
+        self.n = int(n)
+        self.capacity = quantized_capacity(n)
+        self.data = _torch().zeros((2 * self.comps, self.capacity), dtype=_torch().float64, device=device)
+
+    def add(self, expr, atomic=False, stream=None, **low):
+        L = prepare(self, expr, op="accat" if atomic else "acc", **low)
+        L(stream)
+        return self
+
+    def value(self):
+        return Operand(self.data.data_ptr(), self.capacity, "f64", self.shape, owner=self)
+
+    def compensation(self):
+        return Operand(self.data.data_ptr() + self.comps * self.capacity * 8, self.capacity, "f64", self.shape,
+                       owner=self)
+
+    def delivered(self, stream=None):
+        out = Array("f64", self.shape, self.n)
+        assign(out, self.value() + self.compensation(), stream=stream)
+        return out
+
+    def zero(self):
+        self.data.zero_()
+        return self
+
+
 def padded_block_samples(n, parts, pad_to=32):
     """Block pitch of a sample-mode partition: ceil(n / parts) rounded up to
     pad_to (residency/Partition.h:61-72)."""
@@ -354,7 +395,7 @@ class Batch:
 from .runtime import RuntimeOp, runtime_eval, runtime_view  # noqa: E402
 
 __all__ = [
-    "Batch", "RuntimeOp", "runtime_eval", "runtime_view", "padded_block_samples", "partition_view",
+    "Batch", "RuntimeOp", "runtime_eval", "runtime_view", "padded_block_samples", "partition_view", "AccumPlane",
     "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
     "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
     "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",

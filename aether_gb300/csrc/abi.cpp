@@ -390,12 +390,14 @@ bool make_args(const PlanObj* P, const AetherLaunch* a, AgArgsHost& k) {
     bool aligned = true;
     if (pl.wants_store()) {
         if (!a->dst) throw std::runtime_error("plan_launch: null destination");
-        if (pl.dst_comps > 1 && a->dst_pitch < a->n) throw std::runtime_error("plan_launch: destination pitch smaller than n");
+        const int planes = pl.dst_planes();
+        if (planes > 1 && a->dst_pitch && a->dst_pitch < a->n)
+            throw std::runtime_error("plan_launch: destination pitch smaller than n");
         k.dst = static_cast<char*>(a->dst);
         k.dst_pitch = a->dst_pitch ? a->dst_pitch : a->n;
         const int es = ag::dtype_size(pl.dst_dtype);
         aligned = aligned && (reinterpret_cast<uintptr_t>(a->dst) % 16 == 0) &&
-                  (pl.dst_comps == 1 || (k.dst_pitch * es) % 16 == 0);
+                  (planes == 1 || (k.dst_pitch * es) % 16 == 0);
     }
     for (int i = 0; i < pl.n_operands; ++i) {
         const AetherOperand& o = a->operands[i];

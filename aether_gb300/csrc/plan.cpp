@@ -357,8 +357,11 @@ struct Parser {
         plan.dst_shape = parse_shape(tok());
         plan.dst_comps = prod(plan.dst_shape);
         plan.op = tok();
-        if (plan.op != "set" && plan.op != "add" && plan.op != "sub" && plan.op != "sum" && plan.op != "setsum")
+        if (plan.op != "set" && plan.op != "add" && plan.op != "sub" && plan.op != "sum" && plan.op != "setsum" &&
+            plan.op != "acc" && plan.op != "accat")
             fail("unknown assignment '" + plan.op + "'");
+        if (plan.wants_acc() && plan.dst_dtype != DType::F64)
+            fail("accumulation planes are f64 (a value and a compensation plane per component)");
         plan.root = expr();
         expect(")");
         ws();
@@ -859,10 +862,13 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
     }
     const std::string W = g.W, S = g.S;
-    const int OC = P.dst_comps * (dst_ff ? 2 : 1);   // stored planes (ff: hi planes, then lo planes)
-    const bool sum = P.wants_sum(), store = P.wants_store();
-    const bool rw = P.op == "add" || P.op == "sub";
-    if (rw && prec) fail("+= and -= are lowered by the native and emulated-FP64 forms, not the precision form");
+    const int OC = P.dst_planes();   // stored planes (ff: hi then lo; acc: value then compensation)
+    const bool sum = P.wants_sum();
+    const bool atomic_acc = P.op == "accat";
+    const bool store = P.wants_store() && !atomic_acc;   // atomic accumulation writes in the lane loop
+    const bool rw = P.op == "add" || P.op == "sub" || P.op == "acc";
+    if ((rw || atomic_acc) && prec)
+        fail("+=, -= and accumulation are lowered by the native and emulated-FP64 forms, not the precision form");
 
     if (emu) {
         // The native FP64 recomputation of one sample, out of line so its
@@ -899,9 +905,10 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
           << T << ">::load(p" << k << " + c * a.pitch[" << k << "], s0[j], a.n, &in" << k << "[c][j * VEC]);\n";
     }
     if (rw) {
+        const int RC = P.op == "acc" ? OC : P.dst_comps;   // accumulation also reads the compensation planes
         o << "    " << S << "* __restrict__ pd = (" << S << "*)a.dst;\n";
-        o << "    " << S << " cur[" << P.dst_comps << "][L];\n";
-        o << "#pragma unroll\n    for (int c = 0; c < " << P.dst_comps << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, "
+        o << "    " << S << " cur[" << RC << "][L];\n";
+        o << "#pragma unroll\n    for (int c = 0; c < " << RC << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, "
           << S << ">::load_rw(pd + c * a.dst_pitch, s0[j], a.n, &cur[c][j * VEC]);\n";
     }
     // Sample-0 prologue (at0 subtrees): loads of sample 0 and their values.
@@ -957,9 +964,32 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
             o << "        out[" << c << "][l] = (" << S << ")" << v << ";\n";
         } else if (P.op == "add") {
             o << "        out[" << c << "][l] = (" << S << ")ag::rn_add((" << FW << ")cur[" << c << "][l], " << v << ");\n";
+        } else if (P.op == "acc") {
+            // value += term; the exact residual of that sum joins the
+            // compensation plane (accum/atomic.h:141-160)
+            const std::string cv = "cur[" + std::to_string(c) + "][l]";
+            o << "        { const double s_ = ag::rn_add(" << cv << ", " << v << ");\n";
+            o << "          out[" << c << "][l] = s_;\n";
+            o << "          out[" << (P.dst_comps + c) << "][l] = ag::rn_add(cur[" << (P.dst_comps + c)
+              << "][l], ag::two_sum_err(" << cv << ", " << v << ", s_)); }\n";
         } else {
             o << "        out[" << c << "][l] = (" << S << ")ag::rn_sub((" << FW << ")cur[" << c << "][l], " << v << ");\n";
         }
+    }
+    if (atomic_acc) {
+        // concurrent producers: atomicAdd returns the value it added to, so
+        // the residual of each addition is exact and goes to the compensation
+        // plane (the CompensatedAtomic policy of accum/AccumPlane.h)
+        o << "        { const ag_u64 sa_ = s0[l / VEC] + (ag_u64)(l % VEC);\n";
+        o << "          if (sa_ < a.n) {\n";
+        o << "            double* __restrict__ pv_ = (double*)a.dst;\n";
+        for (int c = 0; c < P.dst_comps; ++c) {
+            const std::string v = "(double)fv" + std::to_string(c);
+            o << "            { const double o_ = atomicAdd(pv_ + " << c << " * a.dst_pitch + sa_, " << v << ");\n";
+            o << "              atomicAdd(pv_ + " << (P.dst_comps + c) << " * a.dst_pitch + sa_, ag::two_sum_err(o_, " << v
+              << ", ag::rn_add(o_, " << v << "))); }\n";
+        }
+        o << "          } }\n";
     }
     if (sum) {
         o << "        if (s0[l / VEC] + (ag_u64)(l % VEC) < a.n) ";

@@ -44,6 +44,10 @@ struct Plan {
     bool has_random = false;
     bool wants_sum() const { return op == "sum" || op == "setsum"; }
     bool wants_store() const { return op != "sum"; }
+    // compensated per-sample accumulation: value planes, then compensation planes
+    bool wants_acc() const { return op == "acc" || op == "accat"; }
+    // planes of the destination: float-float and accumulation planes are pairs
+    int dst_planes() const { return dst_comps * ((dst_dtype == DType::FF || wants_acc()) ? 2 : 1); }
 };
 
 // Lowering options (part of the cache key).

@@ -17,6 +17,7 @@
 //   d.download();
 #pragma once
 
+#include "aether/accum.h"
 #include "aether/array.h"
 #include "aether/batch.h"
 #include "aether/device_flag.h"

@@ -53,6 +53,24 @@ int main(int argc, char** argv) {
                     return 1;
                 }
     }
+    // compensated accumulation plane: a + b - a delivers b (to within one ulp)
+    {
+        aether::accum::Plane<3> plane(n);
+        plane += A * 1e6;
+        plane += B;
+        plane += A * -1e6;
+        aether::Array<double, 3> got(n);
+        plane.deliver(got.deviceView());
+        got.download();
+        auto gh = got.hostView();
+        auto bh = b.hostView();
+        for (std::size_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k)
+                if (std::fabs(gh(k, i) - bh(k, i)) > std::fabs(std::nextafter(bh(k, i), 1e300) - bh(k, i))) {
+                    std::printf("accumulation plane mismatch at %zu\n", i);
+                    return 1;
+                }
+    }
     try {
         d.deviceView() = A.dot(B) + aether::constant<aether::extents<2>>(1.0);
         std::printf("shape mismatch was not refused\n");
