@@ -136,6 +136,10 @@ _SIGS = {
     "aether_plan_generate": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.c_char_p,
                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "aether_nvrtc_check": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),
+    "aether_rtc_header_count": (ctypes.c_int, []),
+    "aether_rtc_header": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                         ctypes.POINTER(ctypes.c_char_p)]),
+    "aether_rtc_digest": (ctypes.c_uint64, []),
 }
 
 _lib = None

@@ -682,6 +682,19 @@ AG_EXPORT int aether_plan_generate(const char* ir, const AetherLowering* lowerin
     });
 }
 
+AG_EXPORT int aether_rtc_header_count(void) { return ag::payload_count(); }
+
+AG_EXPORT int aether_rtc_header(int index, const char** name, const char** source) {
+    return guarded([&] {
+        if (!name || !source) throw std::runtime_error("rtc_header: null output pointer");
+        if (!ag::payload_header(index, name, source))
+            throw std::runtime_error("rtc_header: index " + std::to_string(index) + " of " +
+                                     std::to_string(ag::payload_count()));
+    });
+}
+
+AG_EXPORT uint64_t aether_rtc_digest(void) { return ag::payload_digest(); }
+
 AG_EXPORT int aether_nvrtc_check(const char* source, const char* arch) {
     return guarded([&] {
         if (!source || !arch) throw std::runtime_error("nvrtc_check: null argument");

@@ -78,6 +78,28 @@ std::unordered_map<uint64_t, std::string> g_mem;
 
 }  // namespace
 
+int payload_count() { return 3; }
+
+bool payload_header(int i, const char** name, const char** src) {
+    static const char* const names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh"};
+    static const char* const srcs[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc};
+    if (i < 0 || i >= 3) return false;
+    *name = names[i];
+    *src = srcs[i];
+    return true;
+}
+
+uint64_t payload_digest() {
+    uint64_t h = fnv1a(std::string("aether_gb300 rtc payload"));
+    for (int i = 0; i < payload_count(); ++i) {
+        const char *n = nullptr, *s = nullptr;
+        payload_header(i, &n, &s);
+        h = fnv1a(n, h);
+        h = fnv1a(s, h);
+    }
+    return h;
+}
+
 std::string compile_for_arch(const std::string& source, const std::string& arch) {
     const char* hdr_src[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc};
     const char* hdr_names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh"};

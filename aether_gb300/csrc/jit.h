@@ -26,4 +26,10 @@ std::string current_arch();
 // Compile for `arch` without caching or loading (offline checks).
 std::string compile_for_arch(const std::string& source, const std::string& arch);
 
+// The device headers generated kernels include (the NVRTC payload) and a
+// digest of their names and contents.
+int payload_count();
+bool payload_header(int i, const char** name, const char** src);
+uint64_t payload_digest();
+
 }  // namespace ag

@@ -327,6 +327,17 @@ int aether_runtime_eval(int op, const AetherRuntimeView* a, const AetherRuntimeV
  * length into `len`. Stands in for the reference's compile-time type check of
  * an expression (the static_asserts of the expr/nodes headers and expr/Assign.h:205-231). */
 int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* buf, size_t cap, size_t* len);
+/* The NVRTC payload: the device headers every generated kernel includes
+ * (ag_device.cuh: Philox streams, word conversions, native math facade,
+ * compensated-sum primitives; ag_emu64.cuh and its tables: the double-float
+ * arithmetic and functions), for kernels a code generator compiles with its own
+ * NVRTC program and that call the engine's device functions. Replaces the
+ * sealed header payload of dsc/aether_dsc/_core.py:132-200 (names, bytes and a
+ * content digest) over the NVRTC-parseable surface of aether/device.h.
+ * Sources are NUL-terminated, owned by the library, valid until unload. */
+int aether_rtc_header_count(void);
+int aether_rtc_header(int index, const char** name, const char** source);
+uint64_t aether_rtc_digest(void);
 /* Compile `source` with NVRTC for `arch` (e.g. "sm_103a") without loading it;
  * on failure the compiler log is the last error. */
 int aether_nvrtc_check(const char* source, const char* arch);
