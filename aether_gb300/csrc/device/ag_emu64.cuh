@@ -297,7 +297,11 @@ __device__ __forceinline__ df log_s(float s, df x) {
     const float A = __fmul_rn(c, p2f(-e));         // c 2^-e, exact
     const df B = two_sum(__fmul_rn(s, A), -1.0f);   // s A - 1, exact
     const df C = mul(x, A);
-    const df t = add(B, C);
+    // B.lo = 0 whenever B and C can cancel (B = -1 for log; c_i - 1 is exact
+    // by Sterbenz for e = 0), so the two-sum form keeps t to 2^-48 of itself;
+    // for e != 0 the result is >= 0.29 in magnitude and an error of 2^-48 of
+    // the terms is 2^-46.5 of it
+    const df t = add_fast(B, C);
     const df lp = log1p_poly(t);
     const df L = mk(__ldg(&kLogLHi[i]), __ldg(&kLogLLo[i]));
     // e ln2 from a table (the index is clamped; out-of-range e is flagged below)

@@ -445,6 +445,7 @@ struct Gen {
     }
     std::string mulx(int ia, int ib, const std::string& a, const std::string& b) const {
         if (exact_f32(ia) && exact_f32(ib)) return "ag::e64::two_prod(" + a + ".hi, " + b + ".hi)";
+        if (dfm && ia == ib && a == b) return "ag::e64::sqr(" + a + ")";   // x*x: the square's cheaper form
         return mul(a, b);
     }
 
@@ -546,7 +547,7 @@ struct Gen {
         } else if (unary_ops().count(op)) {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x = V(0)[size_t(c)];
-                if (op == "sq") e.push_back(mul(x, x));
+                if (op == "sq") e.push_back(dfm ? "ag::e64::sqr(" + x + ")" : mul(x, x));
                 else if (op == "neg") e.push_back(neg(x));
                 else e.push_back(call(op, {x}, id));
             }
