@@ -282,6 +282,9 @@ __device__ __forceinline__ df log1p_poly(df t) {
     const df s = add_quick(t, scale(t2, -0.5f));
     return add_quick(s, __fmul_rn(t2.hi, q));
 }
+// log_s(s, x) for s + x > 0 with 2^-120 < s + x < 2^120 known in advance
+// (checked = false) skips the validity test.
+template <bool checked = true>
 __device__ __forceinline__ df log_s(float s, df x) {
     const float yh = __fadd_rn(s, x.hi);
     const int bits = __float_as_int(yh);
@@ -292,8 +295,14 @@ __device__ __forceinline__ df log_s(float s, df x) {
         e += 1;
     }
     const float m = __int_as_float(mb);
-    const int i = rint_i(__fmul_rn(__fsub_rn(m, 1.0f), 1024.0f)) + AG_LOG_TAB_OFF;
-    const float c = __ldg(&kLogC[i]);
+    const int i = rint_i(__fmaf_rn(m, 1024.0f, -1024.0f)) + AG_LOG_TAB_OFF;   // (m - 1) 1024, exact
+#ifdef __CUDA_ARCH__
+    const float4 cl = __ldg(reinterpret_cast<const float4*>(kLogCL) + i);
+#else
+    const float* clp = kLogCL + 4 * i;
+    const struct { float x, y, z, w; } cl = {clp[0], clp[1], clp[2], clp[3]};
+#endif
+    const float c = cl.x;
     const float A = __fmul_rn(c, p2f(-e));         // c 2^-e, exact
     const df B = two_sum(__fmul_rn(s, A), -1.0f);   // s A - 1, exact
     const df C = mul(x, A);
@@ -303,18 +312,27 @@ __device__ __forceinline__ df log_s(float s, df x) {
     // the terms is 2^-46.5 of it
     const df t = add_fast(B, C);
     const df lp = log1p_poly(t);
-    const df L = mk(__ldg(&kLogLHi[i]), __ldg(&kLogLLo[i]));
+    const df L = mk(cl.y, cl.z);
     // e ln2 from a table (the index is clamped; out-of-range e is flagged below)
     const int ei = (e < -127 ? -127 : (e > 128 ? 128 : e)) + AG_LN2_TAB_OFF;
-    const df E = mk(__ldg(&kLn2MulHi[ei]), __ldg(&kLn2MulLo[ei]));
+#ifdef __CUDA_ARCH__
+    const float2 ep = __ldg(reinterpret_cast<const float2*>(kLn2Mul) + ei);
+    const df E = mk(ep.x, ep.y);
+#else
+    const df E = mk(kLn2Mul[2 * ei], kLn2Mul[2 * ei + 1]);
+#endif
     // |lp| <= 2^-10.6 <= |L| except for i == 0 (L = 0), and |E| >= ln2 >
     // |L + lp| except for e == 0 (E = 0): each sum is led by its first term.
     const df res = add_quick(E, add_quick(L, lp));
+    if (!checked) return res;
     const bool valid = yh > 0.0f && e > -120 && e < 120;
     return valid ? res : mk(__int_as_float(0x7fc00000), 0.0f);
 }
 __device__ __forceinline__ df log_(df x) { return log_s(0.0f, x); }
 __device__ __forceinline__ df log1p_(df x) { return log_s(1.0f, x); }
+// log1p of an argument known to be >= 0 and below 2^60 (an input in the
+// double-float range, or an expression of such inputs that cannot grow past it)
+__device__ __forceinline__ df log1p_nn_(df x) { return log_s<false>(1.0f, x); }
 
 // ---------------------------------------------------------------------------
 // sin/cos: r in [-pi/4, pi/4] (a little beyond is fine) split as r = j/2048 + t

@@ -83,9 +83,11 @@ def main():
         lh.append(h)
         ll.append(l)
     out.append("#define AG_LOG_TAB_OFF 256")
-    out.append("__device__ const float kLogC[769] = {%s};" % ", ".join(fl(v) for v in cs))
-    out.append("__device__ const float kLogLHi[769] = {%s};" % ", ".join(fl(v) for v in lh))
-    out.append("__device__ const float kLogLLo[769] = {%s};" % ", ".join(fl(v) for v in ll))
+    # packed (c_i, -log c_i hi, lo, 0): one 16-byte load per lookup
+    packed = []
+    for c, h, l in zip(cs, lh, ll):
+        packed += [c, h, l, 0.0]
+    out.append("__device__ __align__(16) const float kLogCL[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
     # ln2 in three parts: the first with 16 bits so e*LN2_1 is exact for |e| < 2^8.
     ln2 = mp.log(2)
     l1 = trunc_bits(ln2, 16)
@@ -94,8 +96,8 @@ def main():
     # e ln2 for e in [-127, 128] as a float pair (the exponent part of a log)
     e_hi, e_lo = zip(*[split2(e * ln2) for e in range(-127, 129)])
     out.append("#define AG_LN2_TAB_OFF 127")
-    out.append("__device__ const float kLn2MulHi[256] = {%s};" % ", ".join(fl(v) for v in e_hi))
-    out.append("__device__ const float kLn2MulLo[256] = {%s};" % ", ".join(fl(v) for v in e_lo))
+    e_pairs = [v for pair in zip(e_hi, e_lo) for v in pair]
+    out.append("__device__ __align__(8) const float kLn2Mul[512] = {%s};" % ", ".join(fl(v) for v in e_pairs))
     out.append("#define AG_LN2_1 %s" % fl(l1))
     out.append("#define AG_LN2_2 %s" % fl(l2))
     out.append("#define AG_LN2_3 %s" % fl(l3))

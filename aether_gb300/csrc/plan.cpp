@@ -471,6 +471,12 @@ struct Gen {
         return "((" + W + ")" + hexlit(v) + ")";
     }
     std::string okv(int id) const { return ctx[size_t(id)] ? "ok0_" : "ok_"; }
+    // |x| of a loaded operand: non-negative and, once the operand passed the
+    // double-float range check, below 2^60
+    bool abs_of_input(int id) const {
+        const Node& n = P.nodes[size_t(id)];
+        return n.op == "abs" && P.nodes[size_t(n.kids[0])].op == "in";
+    }
     // Function spelling; `id` selects the range flag for functions that set one.
     std::string call(const std::string& name, const std::vector<std::string>& args, int id) const {
         std::string a;
@@ -478,6 +484,8 @@ struct Gen {
         if (!dfm) return "ag::f_" + name + "(" + a + ")";
         static const std::set<std::string> own = {"sqrt", "rsqrt", "exp", "log", "log1p", "abs", "sign", "min", "max"};
         if (name == "sin" || name == "cos") return "ag::e64::" + name + "_(" + a + ", " + okv(id) + ")";
+        if (name == "log1p" && abs_of_input(P.nodes[size_t(id)].kids[0]))
+            return "ag::e64::log1p_nn_(" + a + ")";   // |input| is >= 0 and within the input range check
         if (own.count(name)) return "ag::e64::" + name + "_(" + a + ")";
         return "ag::e64::nat_" + name + "(" + a + ")";
     }

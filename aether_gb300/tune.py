@@ -21,8 +21,8 @@ DEFAULT_CANDIDATES = [
     for b in (128, 256, 512)
     for i in (1, 2)
     for v in (0, 1)
-    for m in (0, 3, 4)
-    if not (b == 512 and m == 4)
+    for m in (0, 2, 3, 4)
+    if not (b == 512 and m == 4) and not (b < 512 and m == 2)   # 512 x 2 CTAs caps a thread at 64 registers
 ]
 
 
@@ -39,8 +39,15 @@ def _device_name():
     return torch.cuda.get_device_name(torch.cuda.current_device())
 
 
+def _code_digest():
+    """Digest of the device code every kernel includes: a tuning result stays
+    valid only for the code it was measured on."""
+    from . import _abi
+    return "%016x" % _abi.lib().aether_rtc_digest()
+
+
 def _key(ir, math, contract):
-    h = hashlib.sha1(("%s|%d|%d|%s" % (ir, math, contract, _device_name())).encode()).hexdigest()
+    h = hashlib.sha1(("%s|%d|%d|%s|%s" % (ir, math, contract, _device_name(), _code_digest())).encode()).hexdigest()
     return h
 
 
@@ -51,7 +58,7 @@ def load(include_shipped=True):
     """The user's tuning cache over the winners shipped with the package
     (tuned.json, measured on GB300 for the plans the benchmarks use)."""
     data = {}
-    if include_shipped:
+    if include_shipped and os.environ.get("AETHER_GB300_TUNE_SHIPPED", "1") != "0":
         try:
             with open(SHIPPED) as f:
                 data.update(json.load(f))
