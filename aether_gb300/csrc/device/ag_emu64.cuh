@@ -486,7 +486,8 @@ __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const bool lower = z < (1ull << 52);
     const ag_u64 w = lower ? 2ull * z + 1ull : 2ull * ((1ull << 53) - 1ull - z) + 1ull;
     const df W = scale(from_u64(w), p2f(-54));
-    const df L = log_s(lower ? 0.0f : 1.0f, lower ? W : neg(W));
+    // log(u) for u in [2^-54, 1/2] or log1p(-w) for w in [2^-54, 1/2]: always valid
+    const df L = log_s<false>(lower ? 0.0f : 1.0f, lower ? W : neg(W));
     const df sv = sqrt_(scale(L, -2.0f));
     // v = V 2^-53 with V = 2 zy + 1 odd; reduce v = q/2 + r exactly in integers
     // (q = round(2v), r = R 2^-53, |R| <= 2^51) so sin(pi v) keeps full
