@@ -88,25 +88,12 @@ def main():
     for c, h, l in zip(cs, lh, ll):
         packed += [c, h, l, 0.0]
     out.append("__device__ __align__(16) const float kLogCL[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
-    # ln2 in three parts: the first with 16 bits so e*LN2_1 is exact for |e| < 2^8.
     ln2 = mp.log(2)
-    l1 = trunc_bits(ln2, 16)
-    l2 = trunc_bits(ln2 - l1, 24)
-    l3 = f32(ln2 - l1 - l2)
     # e ln2 for e in [-127, 128] as a float pair (the exponent part of a log)
     e_hi, e_lo = zip(*[split2(e * ln2) for e in range(-127, 129)])
     out.append("#define AG_LN2_TAB_OFF 127")
     e_pairs = [v for pair in zip(e_hi, e_lo) for v in pair]
     out.append("__device__ __align__(8) const float kLn2Mul[512] = {%s};" % ", ".join(fl(v) for v in e_pairs))
-    out.append("#define AG_LN2_1 %s" % fl(l1))
-    out.append("#define AG_LN2_2 %s" % fl(l2))
-    out.append("#define AG_LN2_3 %s" % fl(l3))
-    t3h, t3l = split2(mp.mpf(1) / 3)
-    out.append("#define AG_THIRD_HI %s" % fl(t3h))
-    out.append("#define AG_THIRD_LO %s" % fl(t3l))
-    t6h, t6l = split2(mp.mpf(1) / 6)
-    out.append("#define AG_SIXTH_HI %s" % fl(t6h))
-    out.append("#define AG_SIXTH_LO %s" % fl(t6l))
 
     # --- sin/cos at j/2048, j in [-1664, 1664], packed (S hi, S lo, C hi, C lo) --
     # so one 16-byte load serves a lookup; |r - j/2048| <= 2^-12 leaves the
@@ -130,18 +117,6 @@ def main():
     out.append("#define AG_PIO2_2 %s" % fl(p2))
     out.append("#define AG_PIO2_3 %s" % fl(p3))
     out.append("#define AG_TWO_OVER_PI %s" % fl(2 / mp.pi))
-    # pi/2 as three doubles for the FP64 reduction of large arguments: the
-    # first two with 33 significant bits so k*P for |k| < 2^19 is exact.
-    def trunc_d(v, bits):
-        v = mp.mpf(v)
-        e = mp.floor(mp.log(abs(v), 2))
-        scale = mp.mpf(2) ** (bits - 1 - e)
-        return mp.floor(abs(v) * scale) / scale * mp.sign(v)
-    d1 = trunc_d(pio2, 33)
-    d2 = trunc_d(pio2 - d1, 33)
-    d3 = mp.mpf(float(pio2 - d1 - d2))
-    for name, v in (("AG_PIO2_D1", d1), ("AG_PIO2_D2", d2), ("AG_PIO2_D3", d3)):
-        out.append("#define %s %s" % (name, float(v).hex()))
     pih, pil = split2(mp.pi)
     out.append("#define AG_PI_HI %s" % fl(pih))
     ph2, pl2 = split2(mp.pi / 2)
