@@ -237,10 +237,16 @@ __device__ __forceinline__ df sqrt_(df x) {
     const df res = fast_two_sum(s, __fmul_rn(r, 0.5f * y));
     return x.hi > 0.0f ? res : (x.hi == 0.0f ? mk(0.0f, 0.0f) : mk(__int_as_float(0x7fc00000), 0.0f));
 }
+// One Newton step on a float seed y: e = 1 - x y^2 and rsqrt x = y (1 + e/2).
+// y^2 = p + q exactly (two_prod); x.hi p is within 2^-22 of 1, so fma(-x.hi,
+// p, 1) carries e to 2^-24 of itself and the two smaller products join it by
+// fma; the correction y e / 2 is ~2^-23 of y, so the result is good to ~2^-47.
 __device__ __forceinline__ df rsqrt_(df x) {
     const float y = rsqrt_seed(x.hi);
-    const df xyy = mul(mul(x, y), y);
-    const float e = __fsub_rn(__fsub_rn(1.0f, xyy.hi), xyy.lo);
+    const df yy = two_prod(y, y);
+    float e = __fmaf_rn(-x.hi, yy.hi, 1.0f);
+    e = __fmaf_rn(-x.hi, yy.lo, e);
+    e = __fmaf_rn(-x.lo, yy.hi, e);
     const df res = fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
     return x.hi > 0.0f ? res : mk(__int_as_float(0x7fc00000), 0.0f);
 }
