@@ -417,6 +417,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import aether_gb300 as ag
+    from aether_gb300 import shard
 
     math_mode = args.math
     stream = torch.cuda.current_stream()
@@ -458,10 +459,7 @@ def run_ours(args):
     total_ms = start.elapsed_time(end)
     t_expr = [e[0].elapsed_time(e[1]) for e in ev]
     t_fill = [e[1].elapsed_time(e[2]) for e in ev]
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = shard.max_over_ranks(total_ms, group=dist.group.WORLD if dist else None)
     ms_step = total_ms / args.steps
     value = ws * (BYTES_EXPR + BYTES_FILL) / (ms_step * 1e-3) / 1e9
 
@@ -528,10 +526,7 @@ def run_ours(args):
         for _ in range(e_steps):
             e2e_step()
         e_ms = (time.perf_counter() - t0) * 1e3 / e_steps
-        if dist:
-            t = torch.tensor([e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
+        e_ms = shard.max_over_ranks(e_ms, group=dist.group.WORLD if dist else None)
         e2e = {"value": round(ws * (BYTES_EXPR + BYTES_FILL) / (e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
                "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3),
                "pipeline": "%d sample blocks over 3 streams" % len(chunks)}
