@@ -149,13 +149,21 @@ __device__ __forceinline__ df recip(df y) {
     const float e = __fsub_rn(__fsub_rn(1.0f, yr.hi), yr.lo);
     return fast_two_sum(r, __fmul_rn(r, e));
 }
+// x / y: a float quotient q1 from a twice-refined reciprocal, then one
+// correction from the residual x - y q1, formed exactly enough: y.hi q1 =
+// p.hi + p.lo (two_prod), x.hi - p.hi is exact (Sterbenz: q1 is within 2^-23
+// of the quotient) and the small terms join by fma.
 __device__ __forceinline__ df div(df x, df y) {
-    const float q1 = __fmul_rn(x.hi, rcp_approx(y.hi));
-    const df r = sub(x, mul(y, q1));
-    const float q2 = __fmul_rn(r.hi, rcp_approx(y.hi));
-    const df q = fast_two_sum(q1, q2);
-    const df r2 = sub(x, mul(y, q));
-    return add(q, __fmul_rn(r2.hi, rcp_approx(y.hi)));
+    float r = rcp_approx(y.hi);
+    r = __fmaf_rn(r, __fmaf_rn(-y.hi, r, 1.0f), r);
+    r = __fmaf_rn(r, __fmaf_rn(-y.hi, r, 1.0f), r);   // twice: q1 within ~2^-24, so e's roundings stay at 2^-48 of q
+    const float q1 = __fmul_rn(x.hi, r);
+    const df p = two_prod(y.hi, q1);
+    float e = __fsub_rn(x.hi, p.hi);
+    e = __fsub_rn(e, p.lo);
+    e = __fadd_rn(e, x.lo);
+    e = __fmaf_rn(-y.lo, q1, e);
+    return fast_two_sum(q1, __fmul_rn(e, r));
 }
 
 __device__ __forceinline__ bool gt(df a, df b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
