@@ -103,6 +103,10 @@ _SIGS = {
     "aether_stream_wait": (ctypes.c_int, [ctypes.c_int, _P, _P]),
     "aether_stream_sync": (ctypes.c_int, [ctypes.c_int, _P]),
     "aether_stream_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
+    "aether_current_device": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
+    "aether_pointer_device": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "aether_memory_v1": (_P, []),
+    "aether_gb300_v1": (_P, []),
     "aether_stream_destroy": (None, [_P]),
     "aether_plan_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(AetherLowering), ctypes.POINTER(_P)]),
     "aether_plan_info": (ctypes.c_int, [_P, ctypes.POINTER(AetherPlanInfo)]),

@@ -21,7 +21,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libaether_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp", "serve.cpp"]
+HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp", "serve.cpp", "tables.cpp"]
 DEVICE_SOURCES = ["noalloc.cu", "runtime.cu", "serve_copy.cu"]
 EMBED = [("kAgDeviceSrc", "device/ag_device.cuh"), ("kAgEmu64Src", "device/ag_emu64.cuh"),
          ("kAgEmu64TablesSrc", "device/ag_emu64_tables.cuh")]

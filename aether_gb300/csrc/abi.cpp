@@ -258,6 +258,23 @@ AG_EXPORT int aether_stream_wait(int dev, void* producer, void* consumer) {
     });
 }
 
+AG_EXPORT int aether_current_device(int* dev) {
+    if (!dev) return fail("current_device: null output pointer");
+    const cudaError_t e = cudaGetDevice(dev);
+    return e == cudaSuccess ? AETHER_OK : cuda_fail(e, "cudaGetDevice");
+}
+
+AG_EXPORT int aether_pointer_device(const void* ptr, int* dev) {
+    return guarded([&] {
+        if (!ptr || !dev) throw std::runtime_error("pointer_device: null argument");
+        cudaPointerAttributes at{};
+        ck(cudaPointerGetAttributes(&at, ptr), "cudaPointerGetAttributes");
+        if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+            throw std::runtime_error("pointer_device: not a device pointer");
+        *dev = at.device;
+    });
+}
+
 AG_EXPORT int aether_stream_create(int dev, void** stream) {
     return guarded([&] {
         if (!stream) throw std::runtime_error("stream_create: null output pointer");

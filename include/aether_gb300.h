@@ -58,6 +58,10 @@ int aether_copy(int dst_kind, int dst_dev, void* dst, int src_kind, int src_dev,
 int aether_stream_wait(int dev, void* producer, void* consumer);
 /* dsc/src/seam.h:35 stream_sync. */
 int aether_stream_sync(int dev, void* stream);
+/* dsc/src/seam.h:26 current_device. */
+int aether_current_device(int* dev);
+/* dsc/src/seam.h:36 pointer_device: the device that owns a device pointer. */
+int aether_pointer_device(const void* ptr, int* dev);
 /* No counterpart in the seam, whose callers make cudaStream_t handles with the
  * CUDA runtime (chunk/StreamOrdered.h:38): a non-blocking stream on `dev` for
  * callers that include no CUDA header (graph capture needs one). */
@@ -341,6 +345,79 @@ uint64_t aether_rtc_digest(void);
 /* Compile `source` with NVRTC for `arch` (e.g. "sm_103a") without loading it;
  * on failure the compiler log is the last error. */
 int aether_nvrtc_check(const char* source, const char* arch);
+
+/* ------------------------------------------------------------------------- *
+ * Function tables.
+ *
+ * aether_memory_v1 returns the seam table of dsc/src/seam.h:22-53 with its
+ * exact layout (ABI 2), so the reference's Python loader can open this library
+ * in place of its CUDA plugin. The FFT entries (cuFFT, outside the fused
+ * expression path) answer AETHER_MISSING with a message, the seam's
+ * optional-feature convention.
+ *
+ * aether_gb300_v1 returns the same table plus every entry point of the fused
+ * expression path: one versioned symbol a loader can bind in one call.
+ * ------------------------------------------------------------------------- */
+#define AETHER_MEMORY_ABI 2
+typedef struct AetherMemoryV1 {
+    uint32_t abi;
+    int (*probe)(int* device_count);
+    int (*runtime_version)(int* version);
+    int (*current_device)(int* dev);
+    const char* (*last_error)(void);
+    int (*chunk_alloc)(int kind, int dev, size_t bytes, void* stream, void** chunk, void** ptr);
+    void (*chunk_release)(void* chunk);
+    void (*drain)(void);
+    int (*fill)(int kind, int dev, void* ptr, size_t bytes, const void* value, size_t width, void* stream);
+    int (*copy)(int dst_kind, int dst_dev, void* dst, int src_kind, int src_dev, const void* src, size_t bytes,
+                void* stream);
+    int (*stream_wait)(int dev, void* producer, void* consumer);
+    int (*stream_sync)(int dev, void* stream);
+    int (*pointer_device)(const void* ptr, int* dev);
+    int (*fft_plan)(int dev, int kind, int is_double, int norm, int forward, int ndim, const int64_t* shape, int naxes,
+                    const int32_t* axes, void* stream, void** plan);
+    int (*fft_exec)(void* plan, const void* in, void* out, void* stream);
+    void (*fft_destroy)(void* plan);
+} AetherMemoryV1;
+const AetherMemoryV1* aether_memory_v1(void);
+
+typedef struct AetherGB300V1 {
+    uint32_t abi;   /* AETHER_GB300_ABI */
+    const AetherMemoryV1* memory;
+    int (*stream_create)(int dev, void** stream);
+    void (*stream_destroy)(void* stream);
+    int (*plan_create)(const char* ir, const AetherLowering* lowering, void** plan);
+    int (*plan_info)(void* plan, AetherPlanInfo* info);
+    int (*plan_workspace_size)(void* plan, uint64_t n, uint64_t* bytes);
+    int (*plan_launch)(void* plan, const AetherLaunch* args, void* stream);
+    int (*plan_source)(void* plan, char* buf, size_t cap, size_t* len);
+    void (*plan_release)(void* plan);
+    int (*plan_launch_noalloc)(void* plan, const AetherLaunch* args, void* stream);
+    int (*plan_launch_many)(void* const* plans, const AetherLaunch* args, int count, void* stream);
+    int (*batch_create)(void* const* plans, int n_plans, const AetherLowering* lowering, void** batch);
+    int (*batch_set_items)(void* batch, const AetherBatchItem* items, int n_items, void* stream);
+    int (*batch_launch)(void* batch, void* stream);
+    int (*batch_capture)(void* batch, void* stream);
+    int (*batch_replay)(void* batch, void* stream);
+    int (*batch_info)(void* batch, AetherBatchInfo* info);
+    void (*batch_release)(void* batch);
+    int (*serve_open)(void* const* plans, int n_plans, const AetherServeConfig* config, void** server);
+    int (*serve_submit)(void* server, const AetherServeRequest* request, uint64_t* ticket);
+    int (*serve_feed)(void* server, const AetherServeRequest* requests, int count, uint64_t* tickets);
+    int (*serve_status)(void* server, uint64_t ticket, AetherServeStatus* status);
+    int (*serve_wait)(void* server, uint64_t ticket, double timeout_s, AetherServeStatus* status);
+    int (*serve_release)(void* server, uint64_t ticket);
+    int (*serve_stats)(void* server, AetherServeStats* stats);
+    void (*serve_close)(void* server);
+    int (*runtime_eval)(int op, const AetherRuntimeView* a, const AetherRuntimeView* b, const AetherRuntimeView* out,
+                        double scalar, void* stream);
+    int (*rtc_header_count)(void);
+    int (*rtc_header)(int index, const char** name, const char** source);
+    uint64_t (*rtc_digest)(void);
+    int (*plan_generate)(const char* ir, const AetherLowering* lowering, char* buf, size_t cap, size_t* len);
+    int (*nvrtc_check)(const char* source, const char* arch);
+} AetherGB300V1;
+const AetherGB300V1* aether_gb300_v1(void);
 
 #ifdef __cplusplus
 }

@@ -124,3 +124,48 @@ def test_emulated_math_requires_f64_plan():
     ir = plan_text("f32", (3,), "set", a + a, IrContext())
     src = _abi.generate(ir, _abi.lowering(math=1))
     assert "ag_emu64" in src
+
+
+def test_seam_table_matches_the_reference_layout():
+    """aether_memory_v1 returns the dsc/src/seam.h:22-53 table (ABI 2) whose
+    entries are this library's own functions; FFT answers optional-missing."""
+    import ctypes
+    from aether_gb300 import _abi
+    L = _abi.lib()
+    P = ctypes.c_void_p
+    names = ["probe", "runtime_version", "current_device", "last_error", "chunk_alloc", "chunk_release", "drain",
+             "fill", "copy", "stream_wait", "stream_sync", "pointer_device", "fft_plan", "fft_exec", "fft_destroy"]
+
+    class Mem(ctypes.Structure):
+        _fields_ = [("abi", ctypes.c_uint32)] + [(n, P) for n in names]
+
+    t = ctypes.cast(L.aether_memory_v1(), ctypes.POINTER(Mem)).contents
+    assert t.abi == 2
+    for n in names[:12]:
+        assert t.__getattribute__(n) == ctypes.cast(getattr(L, "aether_" + n), P).value, n
+    fft_plan = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, P, ctypes.c_int, P, P, ctypes.POINTER(P))(t.fft_plan)
+    plan = P(1)
+    assert fft_plan(0, 0, 1, 0, 1, 1, None, 1, None, None, ctypes.byref(plan)) == 2
+    assert plan.value is None and b"FFT" in L.aether_last_error()
+
+
+def test_gb300_table_binds_every_path_entry():
+    import ctypes
+    from aether_gb300 import _abi
+    L = _abi.lib()
+    P = ctypes.c_void_p
+    names = ["stream_create", "stream_destroy", "plan_create", "plan_info", "plan_workspace_size", "plan_launch",
+             "plan_source", "plan_release", "plan_launch_noalloc", "plan_launch_many", "batch_create",
+             "batch_set_items", "batch_launch", "batch_capture", "batch_replay", "batch_info", "batch_release",
+             "serve_open", "serve_submit", "serve_feed", "serve_status", "serve_wait", "serve_release", "serve_stats",
+             "serve_close", "runtime_eval", "rtc_header_count", "rtc_header", "rtc_digest", "plan_generate",
+             "nvrtc_check"]
+
+    class T(ctypes.Structure):
+        _fields_ = [("abi", ctypes.c_uint32), ("memory", P)] + [(n, P) for n in names]
+
+    t = ctypes.cast(L.aether_gb300_v1(), ctypes.POINTER(T)).contents
+    assert t.abi == 1 and t.memory == L.aether_memory_v1()
+    for n in names:
+        assert getattr(t, n) == ctypes.cast(getattr(L, "aether_" + n), P).value, n
