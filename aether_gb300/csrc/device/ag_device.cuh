@@ -196,6 +196,9 @@ struct vec_io<1, T> {
         if (s < n) __stcs(p + s, x[0]);
     }
     static __device__ __forceinline__ void load_rw(const T* p, ag_u64 s, ag_u64 n, T* x) { x[0] = s < n ? p[s] : T(0); }
+    // the whole lane group is inside the range (checked once by the caller)
+    static __device__ __forceinline__ void load_full(const T* p, ag_u64 s, T* x) { x[0] = __ldcs(p + s); }
+    static __device__ __forceinline__ void store_full(T* p, ag_u64 s, const T* x) { __stcs(p + s, x[0]); }
 };
 template <>
 struct vec_io<2, double> {
@@ -226,6 +229,14 @@ struct vec_io<2, double> {
             if (s < n) p[s] = x[0];
             if (s + 1 < n) p[s + 1] = x[1];
         }
+    }
+    static __device__ __forceinline__ void load_full(const double* p, ag_u64 s, double* x) {
+        const double2 v = __ldcs(reinterpret_cast<const double2*>(p + s));
+        x[0] = v.x;
+        x[1] = v.y;
+    }
+    static __device__ __forceinline__ void store_full(double* p, ag_u64 s, const double* x) {
+        __stcs(reinterpret_cast<double2*>(p + s), make_double2(x[0], x[1]));
     }
 };
 template <>
@@ -263,6 +274,16 @@ struct vec_io<4, float> {
                 if (s + v < n) p[s + v] = x[v];
         }
     }
+    static __device__ __forceinline__ void load_full(const float* p, ag_u64 s, float* x) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(p + s));
+        x[0] = v.x;
+        x[1] = v.y;
+        x[2] = v.z;
+        x[3] = v.w;
+    }
+    static __device__ __forceinline__ void store_full(float* p, ag_u64 s, const float* x) {
+        __stcs(reinterpret_cast<float4*>(p + s), make_float4(x[0], x[1], x[2], x[3]));
+    }
 };
 // Mixed widths: a float plane inside a double-width lane group, and the
 // reverse, fall back to two/four scalar accesses.
@@ -283,6 +304,15 @@ struct vec_io<2, float> {
         if (s < n) p[s] = x[0];
         if (s + 1 < n) p[s + 1] = x[1];
     }
+    static __device__ __forceinline__ void load_full(const float* p, ag_u64 s, float* x) {
+        const float2 v = __ldcs(reinterpret_cast<const float2*>(p + s));
+        x[0] = v.x;
+        x[1] = v.y;
+    }
+    static __device__ __forceinline__ void store_full(float* p, ag_u64 s, const float* x) {
+        p[s] = x[0];
+        p[s + 1] = x[1];
+    }
 };
 template <>
 struct vec_io<4, double> {
@@ -297,6 +327,14 @@ struct vec_io<4, double> {
     static __device__ __forceinline__ void store(double* p, ag_u64 s, ag_u64 n, const double* x) {
         vec_io<2, double>::store(p, s, n, x);
         vec_io<2, double>::store(p, s + 2, n, x + 2);
+    }
+    static __device__ __forceinline__ void load_full(const double* p, ag_u64 s, double* x) {
+        vec_io<2, double>::load_full(p, s, x);
+        vec_io<2, double>::load_full(p, s + 2, x + 2);
+    }
+    static __device__ __forceinline__ void store_full(double* p, ag_u64 s, const double* x) {
+        vec_io<2, double>::store_full(p, s, x);
+        vec_io<2, double>::store_full(p, s + 2, x + 2);
     }
 };
 

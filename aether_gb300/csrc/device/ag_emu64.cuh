@@ -103,6 +103,23 @@ __device__ __forceinline__ df sqr(df x) {
     const df c = two_prod(x.hi, x.hi);
     return fast_two_sum(c.hi, __fmaf_rn(2.0f * x.hi, x.lo, c.lo));
 }
+// Products whose only consumer is a sum: the same pair before the final
+// Fast2Sum (|lo| up to about one ulp of hi), which every sum below accepts.
+__device__ __forceinline__ df mul_u(df x, df y) {
+    const df c = two_prod(x.hi, y.hi);
+    const float tl0 = __fmul_rn(x.lo, y.lo);
+    const float tl1 = __fmaf_rn(x.hi, y.lo, tl0);
+    const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
+    return mk(c.hi, __fadd_rn(c.lo, cl2));
+}
+__device__ __forceinline__ df mul_u(df x, float y) {
+    const df c = two_prod(x.hi, y);
+    return mk(c.hi, __fmaf_rn(x.lo, y, c.lo));
+}
+__device__ __forceinline__ df sqr_u(df x) {
+    const df c = two_prod(x.hi, x.hi);
+    return mk(c.hi, __fmaf_rn(2.0f * x.hi, x.lo, c.lo));
+}
 // Scale by an exact power of two.
 __device__ __forceinline__ df scale(df x, float p2) { return mk(__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)); }
 // Sum where the first term dominates: |x.hi| >= |y.hi| (or x == 0), so the
@@ -179,21 +196,28 @@ __device__ __forceinline__ bool ne(df a, df b) { return !eq(a, b); }
 // |x| in [2^-60, 2^60]: the range where products of a few operands stay
 // normal floats.
 __device__ __forceinline__ bool in_range(double x) {
-    const unsigned ex = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
-    return ex - (1023u - 60u) <= 120u;
+    const unsigned ah = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    return ah - (963u << 20) <= (121u << 20) - 1u;
 }
-__device__ __forceinline__ df from_double(double x) {
+// The split of a double, and its range test (the flag is cleared when |x|
+// leaves [2^-60, 2^60]) from the same integer work: the float exponent of the
+// head is the double's less 896, the tail's scale 2^(e-1075) is the head's
+// exponent field less 52 (with the sign carried along).
+__device__ __forceinline__ df from_double_ck(double x, bool& ok) {
     const unsigned h32 = (unsigned)__double2hiint(x);
     const unsigned l32 = (unsigned)__double2loint(x);
-    const unsigned sign = h32 & 0x80000000u;
-    const int ex = (int)((h32 >> 20) & 0x7ffu);
+    const unsigned t = (h32 & 0x7fffffffu) - (896u << 20);
+    ok = ok && t - (67u << 20) <= (121u << 20) - 1u;
     // hi: the top 24 significant bits (truncated), re-biased to float
-    const unsigned hb = ((((h32 & 0x7fffffffu) - (896u << 20)) << 3) | (l32 >> 29)) | sign;
-    // lo: the remaining 29 bits, rounded to a float and scaled by 2^(ex-1075)
-    const float lo = __fmul_rn(__uint2float_rn(l32 & 0x1fffffffu), __int_as_float((ex - 948) << 23));
-    // hi + lo is the double to 2^-48; |lo| < ulp(hi) already, so the pair is
-    // used without renormalising.
-    return mk(__int_as_float(hb), __int_as_float(__float_as_int(lo) ^ sign));
+    const unsigned hb = __funnelshift_l(l32, t, 3) | (h32 & 0x80000000u);
+    // lo: the remaining 29 bits, rounded to a float and scaled by +-2^(ex-1075);
+    // |lo| < ulp(hi), so the pair is used without renormalising
+    const float lo = __fmul_rn(__uint2float_rn(l32 & 0x1fffffffu), __int_as_float((hb & 0xff800000u) - (52u << 23)));
+    return mk(__int_as_float(hb), lo);
+}
+__device__ __forceinline__ df from_double(double x) {
+    bool ok = true;
+    return from_double_ck(x, ok);
 }
 // A normal float (or zero) as a double.
 __device__ __forceinline__ double f2d(float f) {

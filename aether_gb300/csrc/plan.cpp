@@ -443,11 +443,26 @@ struct Gen {
         const Node& n = P.nodes[size_t(id)];
         return dfm && n.op == "in" && n.dtype == DType::F32;
     }
-    std::string mulx(int ia, int ib, const std::string& a, const std::string& b) const {
+    // `u`: the product is read only by sums and may stay unnormalised
+    std::string mulx(bool u, int ia, int ib, const std::string& a, const std::string& b) {
         if (exact_f32(ia) && exact_f32(ib)) return "ag::e64::two_prod(" + a + ".hi, " + b + ".hi)";
-        if (dfm && ia == ib && a == b) return "ag::e64::sqr(" + a + ")";   // x*x: the square's cheaper form
+        if (dfm && ia == ib && a == b) return sqr(u, a);   // x*x: the square's cheaper form
         return mul(a, b);
     }
+    // Nodes read only by sums (add, sub): a square feeding them may stay an
+    // unnormalised pair, saving its final Fast2Sum.
+    std::vector<signed char> sum_only_memo;
+    bool sum_only(int id) {
+        if (sum_only_memo.empty()) {
+            sum_only_memo.assign(P.nodes.size(), 1);
+            sum_only_memo[size_t(P.root)] = 0;
+            for (const Node& m : P.nodes)
+                for (int k : m.kids)
+                    if (m.op != "add" && m.op != "sub") sum_only_memo[size_t(k)] = 0;
+        }
+        return sum_only_memo[size_t(id)] != 0;
+    }
+    std::string sqr(bool u, const std::string& x) { return (u ? "ag::e64::sqr_u(" : "ag::e64::sqr(") + x + ")"; }
 
     std::string add(const std::string& a, const std::string& b) const {
         if (dfm) return "ag::e64::add(" + a + ", " + b + ")";
@@ -532,8 +547,7 @@ struct Gen {
                 } else if (dfm && n.dtype == DType::F32) {
                     e.push_back("ag::e64::mk((float)" + src + ", 0.0f)");   // exact
                 } else if (dfm) {
-                    out_for(id) << "        " << okv(id) << " = " << okv(id) << " && ag::e64::in_range((double)" << src << ");\n";
-                    e.push_back("ag::e64::from_double((double)" + src + ")");
+                    e.push_back("ag::e64::from_double_ck((double)" + src + ", " + okv(id) + ")");
                 } else {
                     e.push_back("(" + W + ")" + src);
                 }
@@ -555,7 +569,7 @@ struct Gen {
         } else if (unary_ops().count(op)) {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x = V(0)[size_t(c)];
-                if (op == "sq") e.push_back(dfm ? "ag::e64::sqr(" + x + ")" : mul(x, x));
+                if (op == "sq") e.push_back(dfm ? sqr(sum_only(id), x) : mul(x, x));
                 else if (op == "neg") e.push_back(neg(x));
                 else e.push_back(call(op, {x}, id));
             }
@@ -567,7 +581,7 @@ struct Gen {
                     e.push_back("ag::e64::add_fast(" + a + ", " + b + ")");
                 else if (op == "add") e.push_back(add(a, b));
                 else if (op == "sub") e.push_back(sub(a, b));
-                else if (op == "mul") e.push_back(mulx(n.kids[0], n.kids[1], a, b));
+                else if (op == "mul") e.push_back(mulx(sum_only(id), n.kids[0], n.kids[1], a, b));
                 else if (op == "div") e.push_back(div(a, b));
                 else e.push_back(call(op, {a, b}, id));
             }
@@ -735,7 +749,7 @@ struct Gen {
             const auto& a = V(0);
             const int m = K(0).comps;
             auto term = [&](int c) -> std::string {
-                if (op == "dot") return mulx(n.kids[0], n.kids[1], a[size_t(c)], V(1)[size_t(c)]);
+                if (op == "dot") return mulx(false, n.kids[0], n.kids[1], a[size_t(c)], V(1)[size_t(c)]);
                 if (op == "sum") return a[size_t(c)];
                 if (op == "maxnorm") return call("abs", {a[size_t(c)]}, id);
                 return mul(a[size_t(c)], a[size_t(c)]);
@@ -753,6 +767,9 @@ struct Gen {
             const bool b0 = K(0).shape.empty();
             const bool b1 = n.kids.size() > 1 && K(1).shape.empty();
             const std::string wp = "(" + W + "*)0";
+            // N(0, 1) with literal parameters: 0 + 1 z is z bit for bit (z != 0)
+            const bool std01 = n.kids.size() > 1 && K(0).op == "lit" && K(0).lit == 0.0 && K(1).op == "lit" &&
+                               K(1).lit == 1.0;
             auto u01 = [&](const char* salt, const std::string& cc) {
                 return dfm ? "ag::e64::draw01_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
                            : "ag::draw01(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
@@ -768,9 +785,10 @@ struct Gen {
                 if (op == "uniform") {   // DistributionLeaf.h:125-131
                     e.push_back(add(x0, mul(sub(x1, x0), u01("AG_SALT_UNIFORM", cc))));
                 } else if (op == "normal") {   // DistributionLeaf.h:192-199
-                    e.push_back(add(x0, mul(x1, nrm("AG_SALT_NORMAL", cc))));
+                    e.push_back(std01 ? nrm("AG_SALT_NORMAL", cc) : add(x0, mul(x1, nrm("AG_SALT_NORMAL", cc))));
                 } else if (op == "lognormal") {   // DistributionLeaf.h:257-264
-                    e.push_back(call("exp", {add(x0, mul(x1, nrm("AG_SALT_LOGNORMAL", cc)))}, id));
+                    e.push_back(call("exp", {std01 ? nrm("AG_SALT_LOGNORMAL", cc)
+                                                   : add(x0, mul(x1, nrm("AG_SALT_LOGNORMAL", cc)))}, id));
                 } else if (op == "exponential") {   // DistributionLeaf.h:329-333
                     e.push_back(div(neg(call("log", {u01("AG_SALT_EXPONENTIAL", cc)}, id)), x0));
                 } else {   // DistributionLeaf.h:380-385
@@ -897,6 +915,8 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     o << "    constexpr int L = AG_IPT * VEC;\n";
     o << "    ag_u64 s0[AG_IPT];\n";
     o << "#pragma unroll\n    for (int j = 0; j < AG_IPT; ++j) s0[j] = chunk * (ag_u64)(AG_BLOCK * AG_IPT * VEC) + ((ag_u64)j * AG_BLOCK + threadIdx.x) * VEC;\n";
+    // One range check for every lane group of the thread (the last is the furthest).
+    o << "    const bool full_ = s0[AG_IPT - 1] + (ag_u64)VEC <= a.n;\n";
     // Loads of every operand used in the lane context.
     std::set<int> lane_ops, zero_ops;
     for (size_t id = 0; id < P.nodes.size(); ++id) {
@@ -910,8 +930,10 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         const int C = P.operand_comps[size_t(k)];
         o << "    const " << T << "* __restrict__ p" << k << " = (const " << T << "*)a.ops[" << k << "];\n";
         o << "    " << T << " in" << k << "[" << C << "][L];\n";
+        o << "    if (full_) {\n#pragma unroll\n    for (int c = 0; c < " << C << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, "
+          << T << ">::load_full(p" << k << " + c * a.pitch[" << k << "], s0[j], &in" << k << "[c][j * VEC]);\n    } else {\n";
         o << "#pragma unroll\n    for (int c = 0; c < " << C << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, "
-          << T << ">::load(p" << k << " + c * a.pitch[" << k << "], s0[j], a.n, &in" << k << "[c][j * VEC]);\n";
+          << T << ">::load(p" << k << " + c * a.pitch[" << k << "], s0[j], a.n, &in" << k << "[c][j * VEC]);\n    }\n";
     }
     if (rw) {
         const int RC = P.op == "acc" ? OC : P.dst_comps;   // accumulation also reads the compensation planes
@@ -930,6 +952,10 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     }
     if (P.has_random) o << "    const ag_u32 g0 = a.offset;\n";
     if (emu) o << "    bool ok0_ = true;\n";
+    // Plain assignments recompute their out-of-range lanes after the stores,
+    // keeping the native call out of the lane loop.
+    const bool defer = emu && P.op == "set" && store;
+    if (defer) o << "    unsigned bad_ = 0u;\n";
     o << g.pro.str();
     if (store) o << "    " << S << " out[" << OC << "][L];\n";
     o << "#pragma unroll\n    for (int l = 0; l < L; ++l) {\n";
@@ -949,7 +975,9 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
             o << "        const " << W << " fv" << c << " = " << root[size_t(c)] << ";\n";
         }
     }
-    if (emu) {
+    if (defer) {
+        o << "        bad_ |= ok_ ? 0u : (1u << l);\n";
+    } else if (emu) {
         // Samples outside the double-float range are recomputed natively.
         o << "        const ag_u64 sl_ = s0[l / VEC] + (ag_u64)(l % VEC);\n";
         o << "        if (!ok_ && sl_ < a.n) {\n            double nv_[" << P.dst_comps << "];\n";
@@ -1008,8 +1036,34 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     o << "    }\n";
     if (store) {
         o << "    " << S << "* __restrict__ po = (" << S << "*)a.dst;\n";
+        o << "    if (full_) {\n#pragma unroll\n    for (int c = 0; c < " << OC << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, " << S
+          << ">::store_full(po + c * a.dst_pitch, s0[j], &out[c][j * VEC]);\n    } else {\n";
         o << "#pragma unroll\n    for (int c = 0; c < " << OC << "; ++c)\n#pragma unroll\n        for (int j = 0; j < AG_IPT; ++j) ag::vec_io<VEC, " << S
-          << ">::store(po + c * a.dst_pitch, s0[j], a.n, &out[c][j * VEC]);\n";
+          << ">::store(po + c * a.dst_pitch, s0[j], a.n, &out[c][j * VEC]);\n    }\n";
+    }
+    if (defer) {
+        // the native recomputation overwrites the lanes the fast path could not serve
+        o << "    if (bad_) {\n        " << S << "* __restrict__ pf_ = (" << S << "*)a.dst;\n";
+        o << "        for (int l = 0; l < L; ++l) {\n";
+        o << "            const ag_u64 sl_ = s0[l / VEC] + (ag_u64)(l % VEC);\n";
+        o << "            if (((bad_ >> l) & 1u) && sl_ < a.n) {\n";
+        o << "                double nv_[" << P.dst_comps << "];\n";
+        o << "                ag_native_lane" << suffix << "(a, sl_, nv_);\n";
+        for (int c = 0; c < P.dst_comps; ++c) {
+            const std::string at = "pf_[(ag_u64)" + std::to_string(c) + " * a.dst_pitch + sl_]";
+            const std::string nv = "nv_[" + std::to_string(c) + "]";
+            if (prec) {
+                o << "                { const ag::e64::df f_ = ag::e64::dfc(" << nv << ");\n";
+                if (dst_ff)
+                    o << "                  " << at << " = f_.hi;\n                  pf_[(ag_u64)" << (P.dst_comps + c)
+                      << " * a.dst_pitch + sl_] = f_.lo; }\n";
+                else
+                    o << "                  " << at << " = __fadd_rn(f_.hi, f_.lo); }\n";
+            } else {
+                o << "                " << at << " = (" << S << ")" << nv << ";\n";
+            }
+        }
+        o << "            }\n        }\n    }\n";
     }
     o << "}\n";
 

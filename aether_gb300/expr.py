@@ -382,7 +382,11 @@ class RandomLeaf(Expr):
         self.op = op
         self.key = key
         self.shape = (vd,)
-        self.params = tuple(p if isinstance(p, Expr) else Scalar(p) for p in params)
+        # N(0, 1) keeps its parameters as literals: the kernel then skips the
+        # affine step 0 + 1 z, which is z bit for bit (a Box-Muller draw is never 0)
+        standard = (op in ("normal", "lognormal") and not any(isinstance(p, Expr) for p in params)
+                    and float(params[0]) == 0.0 and float(params[1]) == 1.0)
+        self.params = tuple(p if isinstance(p, Expr) else (Literal(p) if standard else Scalar(p)) for p in params)
 
     def ir(self, ctx):
         ps = " ".join(p.ir(ctx) for p in self.params)

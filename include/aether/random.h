@@ -30,7 +30,19 @@ inline Expr leaf(const char* op, std::uint64_t key, int vd, std::vector<double> 
     n->op = op;
     n->key = key;
     n->shape = {vd};
-    for (double p : params) n->params.push_back(ir::scalar(p));
+    // N(0, 1) keeps its parameters as literals: the kernel then skips the
+    // affine step 0 + 1 z, which is z bit for bit (a Box-Muller draw is never 0)
+    const bool standard = (std::string(op) == "normal" || std::string(op) == "lognormal") && params.size() == 2 &&
+                          params[0] == 0.0 && params[1] == 1.0;
+    for (double p : params) {
+        if (standard) {
+            auto l = std::make_shared<ir::LiteralNode>();
+            l->v = p;
+            n->params.push_back(l);
+        } else {
+            n->params.push_back(ir::scalar(p));
+        }
+    }
     return Expr(n);
 }
 }  // namespace detail

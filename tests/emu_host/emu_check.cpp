@@ -111,6 +111,22 @@ int main() {
         }
         out.push_back({"cfg2a", s});
     }
+    // the same expression in the generated form: sums of unnormalised
+    // squares, add_fast for sums of non-negative terms, log1p of |input|
+    {
+        Stat s;
+        for (int i = 0; i < N; ++i) {
+            double a = (u01(rng) - 0.5) * 8, b = (u01(rng) - 0.5) * 8, c = (u01(rng) - 0.5) * 8,
+                   d0 = (u01(rng) - 0.5) * 8;
+            bool ok = true;
+            df A = from_double_ck(a, ok), B = from_double_ck(b, ok), C = from_double_ck(c, ok), D = from_double_ck(d0, ok);
+            df r = add_fast(mul(sqrt_(add_fast(sqr_u(A), sqr_u(B))), log1p_nn_(abs_(C))),
+                            rsqrt_(add_fast(dfc(1.0), sqr_u(D))));
+            LD ref = sqrtl((LD)a * a + (LD)b * b) * log1pl(fabsl((LD)c)) + 1.0L / sqrtl(1.0L + (LD)d0 * d0);
+            if (ok) s.add((LD)to_double(r), ref);
+        }
+        out.push_back({"cfg2a_gen", s});
+    }
     // config 1 composite: a + b*c + sin(a)*exp(-c*c)
     {
         Stat s;

@@ -43,6 +43,10 @@ inline int __double2loint(double d) {
     std::memcpy(&u, &d, 8);
     return (int)(uint32_t)u;
 }
+inline unsigned __funnelshift_l(unsigned lo, unsigned hi, unsigned shift) {
+    const unsigned long long w = ((unsigned long long)hi << 32) | lo;
+    return (unsigned)((w << (shift & 31u)) >> 32);
+}
 inline double __hiloint2double(int hi, int lo) {
     uint64_t u = ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo;
     double d;

@@ -23,7 +23,7 @@ from conftest import REPO
 
 BOUNDS = {
     "roundtrip": 33, "sqrt": 256, "rsqrt": 320, "exp_small": 128, "log1p": 160, "log1p_tiny": 256,
-    "log1p_neg": 1024, "sin": 160, "cos": 160, "recip": 384, "mul": 320, "div": 384, "cfg2a": 256,
+    "log1p_neg": 1024, "sin": 160, "cos": 160, "recip": 384, "mul": 320, "div": 384, "cfg2a": 256, "cfg2a_gen": 256,
     "cfg1_termscale": 256, "normal_abs_rel": 256, "trig_large_f32": 256,
 }
 
