@@ -41,6 +41,20 @@ __device__ __forceinline__ df mk(float h, float l) {
     return r;
 }
 
+// One 16-byte table entry (the packed (hi, lo, hi, lo) rows of the tables).
+struct f4 {
+    float x, y, z, w;
+};
+__device__ __forceinline__ f4 ld4(const float* tab, int row) {
+#ifdef __CUDA_ARCH__
+    const float4 v = __ldg(reinterpret_cast<const float4*>(tab) + row);
+    return f4{v.x, v.y, v.z, v.w};
+#else
+    const float* p = tab + 4 * row;
+    return f4{p[0], p[1], p[2], p[3]};
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // Error-free transformations.
 // ---------------------------------------------------------------------------
@@ -82,6 +96,12 @@ __device__ __forceinline__ df add_fast(df x, df y) {
     const df s = two_sum(x.hi, y.hi);
     const float v = __fadd_rn(__fadd_rn(x.lo, y.lo), s.lo);
     return fast_two_sum(s.hi, v);
+}
+// The same sum left unnormalised, for a value whose only reader is the
+// reassembly into a double (which rounds hi + lo once either way).
+__device__ __forceinline__ df add_fast_u(df x, df y) {
+    const df s = two_sum(x.hi, y.hi);
+    return mk(s.hi, __fadd_rn(__fadd_rn(x.lo, y.lo), s.lo));
 }
 __device__ __forceinline__ df add(df x, float y) {
     const df s = two_sum(x.hi, y);
@@ -261,12 +281,21 @@ __device__ __forceinline__ float rsqrt_seed(float x) {
     const float e = __fmaf_rn(-__fmul_rn(x, y), y, 1.0f);
     return __fmaf_rn(__fmul_rn(0.5f, y), e, y);
 }
-__device__ __forceinline__ df sqrt_(df x) {
+// x > 0 (no zero, negative or NaN argument can reach it)
+__device__ __forceinline__ df sqrt_pos_(df x) {
     const float y = rsqrt_seed(x.hi);
     const float s = __fmul_rn(x.hi, y);
     const df p = two_prod(s, s);
     const float r = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p.hi), p.lo), x.lo);
-    const df res = fast_two_sum(s, __fmul_rn(r, 0.5f * y));
+    return fast_two_sum(s, __fmul_rn(r, 0.5f * y));
+}
+// x >= 0 or NaN (a sum of squares): zero keeps its own branch
+__device__ __forceinline__ df sqrt_nn_(df x) {
+    const df res = sqrt_pos_(x);
+    return x.hi == 0.0f ? mk(0.0f, 0.0f) : res;
+}
+__device__ __forceinline__ df sqrt_(df x) {
+    const df res = sqrt_pos_(x);
     return x.hi > 0.0f ? res : (x.hi == 0.0f ? mk(0.0f, 0.0f) : mk(__int_as_float(0x7fc00000), 0.0f));
 }
 // One Newton step on a float seed y: e = 1 - x y^2 and rsqrt x = y (1 + e/2).
@@ -324,8 +353,13 @@ __device__ __forceinline__ df log1p_poly(df t) {
     return add_quick(s, __fmul_rn(t2.hi, q));
 }
 // log_s(s, x) for s + x > 0 with 2^-120 < s + x < 2^120 known in advance
-// (checked = false) skips the validity test.
-template <bool checked = true>
+// (checked = false) skips the validity test. MODE selects how the reduced
+// argument t = s A - 1 + x A is formed: 0 for log (s = 0: x.hi A is within
+// 2^-10 of 1, so x.hi A - 1 is exact by Sterbenz), 1 for log1p (s = 1:
+// A - 1 as an exact two-sum), 2 for s in {0, 1} at run time where s A - 1 is
+// a single exact FMA (s = 1 only with 1/2 <= s + x < 1, A in [2/3, 2]).
+enum { LOG_S0 = 0, LOG_S1 = 1, LOG_SRT = 2 };
+template <bool checked = true, int MODE = LOG_S1>
 __device__ __forceinline__ df log_s(float s, df x) {
     const float yh = __fadd_rn(s, x.hi);
     const int bits = __float_as_int(yh);
@@ -337,21 +371,27 @@ __device__ __forceinline__ df log_s(float s, df x) {
     }
     const float m = __int_as_float(mb);
     const int i = rint_i(__fmaf_rn(m, 1024.0f, -1024.0f)) + AG_LOG_TAB_OFF;   // (m - 1) 1024, exact
-#ifdef __CUDA_ARCH__
-    const float4 cl = __ldg(reinterpret_cast<const float4*>(kLogCL) + i);
-#else
-    const float* clp = kLogCL + 4 * i;
-    const struct { float x, y, z, w; } cl = {clp[0], clp[1], clp[2], clp[3]};
-#endif
+    const f4 cl = ld4(kLogCL, i);
     const float c = cl.x;
     const float A = __fmul_rn(c, p2f(-e));         // c 2^-e, exact
-    const df B = two_sum(__fmul_rn(s, A), -1.0f);   // s A - 1, exact
-    const df C = mul(x, A);
-    // B.lo = 0 whenever B and C can cancel (B = -1 for log; c_i - 1 is exact
-    // by Sterbenz for e = 0), so the two-sum form keeps t to 2^-48 of itself;
-    // for e != 0 the result is >= 0.29 in magnitude and an error of 2^-48 of
-    // the terms is 2^-46.5 of it
-    const df t = add_fast(B, C);
+    // x A = p + (x.lo A + p.lo), the pair left unnormalised for the sum
+    const df p = two_prod(x.hi, A);
+    const float pl = __fmaf_rn(x.lo, A, p.lo);
+    df t;
+    if (MODE == LOG_S0) {
+        t = fast_two_sum(__fsub_rn(p.hi, 1.0f), pl);
+    } else if (MODE == LOG_SRT) {
+        const df u = two_sum(__fmaf_rn(s, A, -1.0f), p.hi);
+        t = fast_two_sum(u.hi, __fadd_rn(pl, u.lo));
+    } else {
+        // B = A - 1 exactly; B.lo = 0 whenever B and x A can cancel (c_i - 1
+        // is exact by Sterbenz for e = 0), so t keeps 2^-48 of itself there;
+        // for e != 0 the result is >= 0.29 in magnitude and an error of 2^-48
+        // of the terms is 2^-46.5 of it
+        const df B = two_sum(A, -1.0f);
+        const df u = two_sum(B.hi, p.hi);
+        t = fast_two_sum(u.hi, __fadd_rn(__fadd_rn(B.lo, pl), u.lo));
+    }
     const df lp = log1p_poly(t);
     const df L = mk(cl.y, cl.z);
     // e ln2 from a table (the index is clamped; out-of-range e is flagged below)
@@ -369,11 +409,11 @@ __device__ __forceinline__ df log_s(float s, df x) {
     const bool valid = yh > 0.0f && e > -120 && e < 120;
     return valid ? res : mk(__int_as_float(0x7fc00000), 0.0f);
 }
-__device__ __forceinline__ df log_(df x) { return log_s(0.0f, x); }
-__device__ __forceinline__ df log1p_(df x) { return log_s(1.0f, x); }
+__device__ __forceinline__ df log_(df x) { return log_s<true, LOG_S0>(0.0f, x); }
+__device__ __forceinline__ df log1p_(df x) { return log_s<true, LOG_S1>(1.0f, x); }
 // log1p of an argument known to be >= 0 and below 2^60 (an input in the
 // double-float range, or an expression of such inputs that cannot grow past it)
-__device__ __forceinline__ df log1p_nn_(df x) { return log_s<false>(1.0f, x); }
+__device__ __forceinline__ df log1p_nn_(df x) { return log_s<false, LOG_S1>(1.0f, x); }
 
 // ---------------------------------------------------------------------------
 // sin/cos: r in [-pi/4, pi/4] (a little beyond is fine) split as r = j/2048 + t
@@ -388,21 +428,12 @@ __device__ __forceinline__ df log1p_nn_(df x) { return log_s<false>(1.0f, x); }
 // quadrant, and both are A (1 + cm1) + B st with the table pair (A, B) =
 // (S_j, C_j) for sin r and (C_j, -S_j) for cos r, so only the wanted one is
 // evaluated.
-__device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
-    int j = rint_i(__fmul_rn(r.hi, 2048.0f));
-    j = j < -AG_SC_TAB_OFF ? -AG_SC_TAB_OFF : (j > AG_SC_TAB_OFF ? AG_SC_TAB_OFF : j);   // NaN-safe index
-    const float jf = (float)j;
-    const df t = fast_two_sum(__fsub_rn(r.hi, __fmul_rn(jf, 4.8828125e-4f)), r.lo);   // exact first difference
+// The table step for x = q pi/2 + a + t, with sc = (sin a, cos a) from a table.
+__device__ __forceinline__ df trig_tail(const f4& sc, df t, int q, bool want_cos) {
     const float th = t.hi;
     const float th2 = __fmul_rn(th, th);
     const float cubic = __fmul_rn(__fmul_rn(th, th2), __fmaf_rn(th2, 8.33333333e-3f, -1.66666667e-1f));
     const float cm1 = __fmul_rn(th2, __fmaf_rn(th2, 4.16666667e-2f, -0.5f));
-#ifdef __CUDA_ARCH__
-    const float4 sc = __ldg(reinterpret_cast<const float4*>(kSinCos2048) + (j + AG_SC_TAB_OFF));
-#else
-    const float* scp = kSinCos2048 + 4 * (j + AG_SC_TAB_OFF);
-    const struct { float x, y, z, w; } sc = {scp[0], scp[1], scp[2], scp[3]};
-#endif
     const int qq = (q + (want_cos ? 1 : 0)) & 3;   // cos x = sin(x + pi/2)
     const bool odd = qq & 1;
     const df A = odd ? mk(sc.z, sc.w) : mk(sc.x, sc.y);
@@ -411,6 +442,13 @@ __device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
     // the sum is led by A
     const df v = add_quick(add_quick(A, mul(B, t)), __fmaf_rn(A.hi, cm1, __fmul_rn(B.hi, cubic)));
     return (qq & 2) ? neg(v) : v;
+}
+__device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
+    int j = rint_i(__fmul_rn(r.hi, 2048.0f));
+    j = j < -AG_SC_TAB_OFF ? -AG_SC_TAB_OFF : (j > AG_SC_TAB_OFF ? AG_SC_TAB_OFF : j);   // NaN-safe index
+    const float jf = (float)j;
+    const df t = fast_two_sum(__fsub_rn(r.hi, __fmul_rn(jf, 4.8828125e-4f)), r.lo);   // exact first difference
+    return trig_tail(ld4(kSinCos2048, j + AG_SC_TAB_OFF), t, q, want_cos);
 }
 // Cody-Waite reduction by pi/2; valid for |k| < 4096, flagged otherwise.
 __device__ __forceinline__ df dfc(double x);
@@ -521,6 +559,8 @@ __device__ __forceinline__ df draw01_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag_u32 w = ag::philox_block(seed, g, c).x;
     return scale(from_u64(2ull * w + 1ull), p2f(-33));
 }
+// U: the product is left unnormalised (the draw is only reassembled into a double)
+template <bool U = false>
 __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag::q4 x = ag::philox_block(seed, g, c);
     const ag_u64 z = (ag_u64)x.x ^ ((ag_u64)x.y << 21);
@@ -528,17 +568,25 @@ __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag_u64 w = lower ? 2ull * z + 1ull : 2ull * ((1ull << 53) - 1ull - z) + 1ull;
     const df W = scale(from_u64(w), p2f(-54));
     // log(u) for u in [2^-54, 1/2] or log1p(-w) for w in [2^-54, 1/2]: always valid
-    const df L = log_s<false>(lower ? 0.0f : 1.0f, lower ? W : neg(W));
-    const df sv = sqrt_(scale(L, -2.0f));
-    // v = V 2^-53 with V = 2 zy + 1 odd; reduce v = q/2 + r exactly in integers
-    // (q = round(2v), r = R 2^-53, |R| <= 2^51) so sin(pi v) keeps full
-    // relative accuracy next to the zeros of the sine.
+    const df L = log_s<false, LOG_SRT>(lower ? 0.0f : 1.0f, lower ? W : neg(W));
+    const df sv = sqrt_pos_(scale(L, -2.0f));   // log u < 0: the argument is positive
+    // v = V 2^-53 with V = 2 zy + 1 odd, V < 2^54. In integers: K = round(V /
+    // 2^41) counts steps of 1/4096 half-turn, q = round(K / 2048) is the
+    // quadrant, j = K - 2048 q in [-1024, 1024] the table point pi j/4096,
+    // and R = V - 2^41 K (|R| <= 2^40) the remainder, exact in a double-float:
+    // sin(pi v) keeps full relative accuracy next to the zeros of the sine.
     const ag_u64 zy = (ag_u64)x.z ^ ((ag_u64)x.w << 21);
     const ag_u64 V = 2ull * zy + 1ull;
-    const ag_u64 q = (V + (1ull << 51)) >> 52;
-    const ag_i64 R = (ag_i64)V - (ag_i64)(q << 52);
-    const df ra = scale(from_u64((ag_u64)(R < 0 ? -R : R)), p2f(-53));
-    return mul(sv, trig_core(mul(R < 0 ? neg(ra) : ra, mk(AG_PI_HI, AG_PI_LO)), (int)q, false));
+    const ag_u32 vh = (ag_u32)(V >> 32), vl = (ag_u32)V;
+    const ag_u32 K = (vh + 256u) >> 9;   // (V + 2^40) >> 41
+    const int q = (int)((K + 1024u) >> 11);
+    const int j = (int)K - (q << 11);
+    const ag_u32 rh = vh - (K << 9);   // R = rh 2^32 + vl, rh in [-256, 255] as a signed word
+    // R = Rh 2^17 + Rl with Rh = floor(R / 2^17) (|Rh| <= 2^23) and 0 <= Rl < 2^17
+    const int Rh = (int)((rh << 15) | (vl >> 17));
+    const df t = fast_two_sum(__fmul_rn((float)Rh, p2f(-36)), __fmul_rn((float)(vl & 0x1ffffu), p2f(-53)));
+    const df sn = trig_tail(ld4(kSinCosPi4096, j + AG_SCPI_TAB_OFF), mul(t, mk(AG_PI_HI, AG_PI_LO)), q, false);
+    return U ? mul_u(sv, sn) : mul(sv, sn);
 }
 
 // ---------------------------------------------------------------------------

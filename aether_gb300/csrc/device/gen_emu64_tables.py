@@ -108,6 +108,15 @@ def main():
         out.append("#define AG_2OPI_W%d 0x%016xull" % (k, w))
     out.append("#define AG_SC_TAB_OFF 1664")
     out.append("__device__ __align__(16) const float kSinCos2048[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
+    # sin/cos(pi j/4096), j in [-1024, 1024], packed like the table above: the
+    # Box-Muller angle pi v is reduced in integers to a quadrant, one of these
+    # points and an exact remainder of at most pi 2^-13.
+    packed = []
+    for j in range(-1024, 1025):
+        a = mp.pi * mp.mpf(j) / 4096
+        packed += list(split2(mp.sin(a))) + list(split2(mp.cos(a)))
+    out.append("#define AG_SCPI_TAB_OFF 1024")
+    out.append("__device__ __align__(16) const float kSinCosPi4096[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
     # pi/2 in three parts: the first with 12 bits so k*P1 is exact for |k| < 2^12.
     pio2 = mp.pi / 2
     p1 = trunc_bits(pio2, 12)

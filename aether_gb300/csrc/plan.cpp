@@ -450,12 +450,15 @@ struct Gen {
         return mul(a, b);
     }
     // Nodes read only by sums (add, sub): a square feeding them may stay an
-    // unnormalised pair, saving its final Fast2Sum.
+    // unnormalised pair, saving its final Fast2Sum. The root of an emulated
+    // FP64 plan is read only by the reassembly into a double, which rounds
+    // hi + lo once whether or not the pair is normalised.
+    bool root_to_double = false;
     std::vector<signed char> sum_only_memo;
     bool sum_only(int id) {
         if (sum_only_memo.empty()) {
             sum_only_memo.assign(P.nodes.size(), 1);
-            sum_only_memo[size_t(P.root)] = 0;
+            sum_only_memo[size_t(P.root)] = root_to_double ? 1 : 0;
             for (const Node& m : P.nodes)
                 for (int k : m.kids)
                     if (m.op != "add" && m.op != "sub") sum_only_memo[size_t(k)] = 0;
@@ -570,6 +573,7 @@ struct Gen {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x = V(0)[size_t(c)];
                 if (op == "sq") e.push_back(dfm ? sqr(sum_only(id), x) : mul(x, x));
+                else if (op == "sqrt" && dfm && nonneg(n.kids[0])) e.push_back("ag::e64::sqrt_nn_(" + x + ")");
                 else if (op == "neg") e.push_back(neg(x));
                 else e.push_back(call(op, {x}, id));
             }
@@ -578,7 +582,8 @@ struct Gen {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string a = V(0)[size_t(c)], b = V(1)[size_t(c)];
                 if (op == "add" && dfm && nonneg(n.kids[0]) && nonneg(n.kids[1]))
-                    e.push_back("ag::e64::add_fast(" + a + ", " + b + ")");
+                    e.push_back((root_to_double && id == P.root ? "ag::e64::add_fast_u(" : "ag::e64::add_fast(") + a +
+                                ", " + b + ")");
                 else if (op == "add") e.push_back(add(a, b));
                 else if (op == "sub") e.push_back(sub(a, b));
                 else if (op == "mul") e.push_back(mulx(sum_only(id), n.kids[0], n.kids[1], a, b));
@@ -774,8 +779,10 @@ struct Gen {
                 return dfm ? "ag::e64::draw01_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
                            : "ag::draw01(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
             };
+            const bool nrm_u = std01 && root_to_double && id == P.root && n.op == "normal";
             auto nrm = [&](const char* salt, const std::string& cc) {
-                return dfm ? "ag::e64::normal_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
+                return dfm ? std::string(nrm_u ? "ag::e64::normal_df<true>(" : "ag::e64::normal_df(") + key + " ^ " +
+                                 salt + ", " + gid + ", " + cc + ")"
                            : "ag::drawn(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
             };
             for (int c = 0; c < n.comps; ++c) {
@@ -872,6 +879,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     const bool dst_ff = P.dst_dtype == DType::FF;
     if (dst_ff && !prec) fail("ff destinations are written by the precision form (math = 2)");
     Gen g(P, low, ctx, emu, emu ? "d" : "t");
+    g.root_to_double = emu && P.dst_dtype == DType::F64;
     const std::vector<std::string> root = g.emit(P.root);
     Lowering nat = low;
     nat.math = 0;

@@ -120,7 +120,7 @@ int main() {
                    d0 = (u01(rng) - 0.5) * 8;
             bool ok = true;
             df A = from_double_ck(a, ok), B = from_double_ck(b, ok), C = from_double_ck(c, ok), D = from_double_ck(d0, ok);
-            df r = add_fast(mul(sqrt_(add_fast(sqr_u(A), sqr_u(B))), log1p_nn_(abs_(C))),
+            df r = add_fast_u(mul(sqrt_nn_(add_fast(sqr_u(A), sqr_u(B))), log1p_nn_(abs_(C))),
                             rsqrt_(add_fast(dfc(1.0), sqr_u(D))));
             LD ref = sqrtl((LD)a * a + (LD)b * b) * log1pl(fabsl((LD)c)) + 1.0L / sqrtl(1.0L + (LD)d0 * d0);
             if (ok) s.add((LD)to_double(r), ref);
@@ -157,6 +157,8 @@ int main() {
             const LD v = ((LD)zy + 0.5L) * 2.2204460492503130808e-16L;
             const LD ref = sqrtl(-2.0L * logl(u)) * sinl(v * 3.14159265358979323846264338327950288L);
             const double got = to_double(normal_df(seed, (ag_u32)i, 0u));
+            // the unnormalised form reassembles to the same double
+            if (to_double(normal_df<true>(seed, (ag_u32)i, 0u)) != got) ++s.bad;
             // TIER-TOL form: |got - ref| / (1 + |ref|)
             LD e = fabsl((LD)got - ref) / (1.0L + fabsl(ref)) / U;
             if (e > s.max_rel) s.max_rel = (double)e;
