@@ -470,7 +470,7 @@ __device__ __forceinline__ df trig_tail(const f4& sc, df t, int q, bool want_cos
     const df B = odd ? mk(-sc.x, -sc.y) : mk(sc.z, sc.w);
     // |A| >= sin(2^-11) >= 2 |B t| for j != 0, and A = 0 at j = 0 for sin r:
     // the sum is led by A
-    const df v = add_quick(add_quick(A, mul(B, t)), __fmaf_rn(A.hi, cm1, __fmul_rn(B.hi, cubic)));
+    const df v = add_quick(add_quick(A, mul_u(B, t)), __fmaf_rn(A.hi, cm1, __fmul_rn(B.hi, cubic)));
     return (qq & 2) ? neg(v) : v;
 }
 __device__ __forceinline__ df trig_core(df r, int q, bool want_cos) {
