@@ -167,6 +167,43 @@ def run_reference(args):
     return 0
 
 
+def link_rates(L, dev, h_in, a_in, h_out, a_out, nbytes, s_up, s_down):
+    """Host->device, device->host and two-way copy rates (GB/s) of pinned
+    buffers through aether_copy, timed with events on the copy streams."""
+    import ctypes
+    import torch
+    up, down = ctypes.c_void_p(s_up.cuda_stream), ctypes.c_void_p(s_down.cuda_stream)
+    src_in, dst_in = ctypes.c_void_p(h_in.data_ptr()), ctypes.c_void_p(a_in.data.data_ptr())
+    src_out, dst_out = ctypes.c_void_p(a_out.data.data_ptr()), ctypes.c_void_p(h_out.data_ptr())
+
+    def one(do_up, do_down):
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(s_up)
+            s_down.wait_event(e0)
+            if do_up:
+                ag_check(L.aether_copy(1, dev, dst_in, 2, 0, src_in, nbytes, up))
+            if do_down:
+                ag_check(L.aether_copy(2, 0, dst_out, 1, dev, src_out, nbytes, down))
+            e1.record(s_down)
+            s_up.wait_event(e1)
+            e2.record(s_up)
+            e2.synchronize()
+            ms = e0.elapsed_time(e2)
+            best = ms if best is None else min(best, ms)
+        return (int(do_up) + int(do_down)) * nbytes / (best * 1e-3) / 1e9
+
+    return {"h2d_gbs": round(one(True, False), 1), "d2h_gbs": round(one(False, True), 1),
+            "both_gbs": round(one(True, True), 1), "bytes_each_way": nbytes}
+
+
+def ag_check(rc):
+    from aether_gb300 import _abi
+    _abi.check(rc)
+
+
 def _time_ms(fn, reps=5, warmup=2):
     import torch
     for _ in range(warmup):
@@ -474,11 +511,16 @@ def run_ours(args):
             h.copy_(x.data[:, :N_EXPR])
         host_out = torch.empty((3, N_EXPR), dtype=torch.float64, pin_memory=True)
         host_fill = torch.empty((1, N_FILL), dtype=torch.float64, pin_memory=True)
-        # The step cut into K sample blocks (partition_view), each block's
-        # uploads, kernels and downloads on one of three streams, so block
-        # r+1 copies in while block r computes and block r-1 copies out.
+        # The step cut into K sample blocks (partition_view) through a
+        # three-stage pipeline: uploads on one stream, kernels on a second,
+        # downloads on a third, joined by events, so block r+1 copies in
+        # while block r computes and block r-1 copies out, and neither copy
+        # direction waits behind the other.
         K = max(1, args.e2e_chunks)
         streams = [torch.cuda.Stream() for _ in range(3)]
+        s_up, s_run, s_down = streams
+        ev_up = [torch.cuda.Event() for _ in range(K)]
+        ev_run = [torch.cuda.Event() for _ in range(K)]
         pitch_e = ag.padded_block_samples(N_EXPR, K)
         pitch_f = ag.padded_block_samples(N_FILL, K)
         chunks = []
@@ -497,25 +539,28 @@ def run_ours(args):
             chunks.append((r * pitch_e, bo.n, r * pitch_f, bz.n, ke, kf))
         cap = arrs[0].capacity
 
+        up_p, down_p = ctypes.c_void_p(s_up.cuda_stream), ctypes.c_void_p(s_down.cuda_stream)
+
         def e2e_step():
             for k, (e0, en, f0, fn, ke, kf) in enumerate(chunks):
-                st = streams[k % len(streams)]
-                sp = ctypes.c_void_p(st.cuda_stream)
                 for h, x in zip(host_in, arrs):
                     for c in range(3):
                         ag._abi.check(L.aether_copy(1, local, ctypes.c_void_p(x.data.data_ptr() + (c * cap + e0) * 8), 2, 0,
-                                                    ctypes.c_void_p(h.data_ptr() + (c * N_EXPR + e0) * 8), en * 8, sp))
+                                                    ctypes.c_void_p(h.data_ptr() + (c * N_EXPR + e0) * 8), en * 8, up_p))
+                ev_up[k].record(s_up)
+                s_run.wait_event(ev_up[k])
                 if ke is not None:
-                    ke(st.cuda_stream)
+                    ke(s_run.cuda_stream)
                 if kf is not None:
-                    kf(st.cuda_stream)
+                    kf(s_run.cuda_stream)
+                ev_run[k].record(s_run)
+                s_down.wait_event(ev_run[k])
                 for c in range(3):
                     ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_out.data_ptr() + (c * N_EXPR + e0) * 8), 1,
-                                                local, ctypes.c_void_p(d.data.data_ptr() + (c * cap + e0) * 8), en * 8, sp))
+                                                local, ctypes.c_void_p(d.data.data_ptr() + (c * cap + e0) * 8), en * 8, down_p))
                 ag._abi.check(L.aether_copy(2, 0, ctypes.c_void_p(host_fill.data_ptr() + f0 * 8), 1, local,
-                                            ctypes.c_void_p(z.data.data_ptr() + f0 * 8), fn * 8, sp))
-            for st in streams:
-                ag._abi.check(L.aether_stream_sync(local, ctypes.c_void_p(st.cuda_stream)))
+                                            ctypes.c_void_p(z.data.data_ptr() + f0 * 8), fn * 8, down_p))
+            ag._abi.check(L.aether_stream_sync(local, down_p))
 
         e2e_step()
         torch.cuda.synchronize()
@@ -529,7 +574,17 @@ def run_ours(args):
         e_ms = shard.max_over_ranks(e_ms, group=dist.group.WORLD if dist else None)
         e2e = {"value": round(ws * (BYTES_EXPR + BYTES_FILL) / (e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
                "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3),
-               "pipeline": "%d sample blocks over 3 streams" % len(chunks)}
+               "pipeline": "%d sample blocks: upload, compute and download streams" % len(chunks)}
+        # The host link measured in the same process: one large copy each
+        # way, then both at once; the copy time of one step at those rates
+        # is the bound the end-to-end number is read against.
+        link = link_rates(L, local, host_in[0], arrs[0], host_out, d, nb, s_up, s_down)
+        h2d_b, d2h_b = 4 * nb, nb + N_FILL * 8
+        bound_ms = 1e3 * max(h2d_b / (link["h2d_gbs"] * 1e9), d2h_b / (link["d2h_gbs"] * 1e9),
+                             (h2d_b + d2h_b) / (link["both_gbs"] * 1e9))
+        link["step_copy_bound_ms"] = round(bound_ms, 3)
+        link["frac"] = round(bound_ms / e_ms, 3)
+        e2e["link"] = link
 
     if rank != 0:
         if dist:
