@@ -300,15 +300,13 @@ __device__ __forceinline__ df sqrt_pos_(df x) {
     const float r = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p.hi), p.lo), x.lo);
     return fast_two_sum(s, __fmul_rn(r, 0.5f * y));
 }
-// x >= 0 or NaN (a sum of squares): zero keeps its own branch
-__device__ __forceinline__ df sqrt_nn_(df x) {
+// Any argument: a negative or NaN one makes the seed NaN and with it the
+// pair; zero (where seed times argument is 0 x inf) keeps its own branch.
+__device__ __forceinline__ df sqrt_(df x) {
     const df res = sqrt_pos_(x);
     return x.hi == 0.0f ? mk(0.0f, 0.0f) : res;
 }
-__device__ __forceinline__ df sqrt_(df x) {
-    const df res = sqrt_pos_(x);
-    return x.hi > 0.0f ? res : (x.hi == 0.0f ? mk(0.0f, 0.0f) : mk(__int_as_float(0x7fc00000), 0.0f));
-}
+__device__ __forceinline__ df sqrt_nn_(df x) { return sqrt_(x); }
 // One Newton step on a float seed y: e = 1 - x y^2 and rsqrt x = y (1 + e/2).
 // y^2 = p + q exactly (two_prod); x.hi p is within 2^-22 of 1, so fma(-x.hi,
 // p, 1) carries e to 2^-24 of itself and the two smaller products join it by
@@ -319,8 +317,9 @@ __device__ __forceinline__ df rsqrt_(df x) {
     float e = __fmaf_rn(-x.hi, yy.hi, 1.0f);
     e = __fmaf_rn(-x.hi, yy.lo, e);
     e = __fmaf_rn(-x.lo, yy.hi, e);
-    const df res = fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
-    return x.hi > 0.0f ? res : mk(__int_as_float(0x7fc00000), 0.0f);
+    // x.hi <= 0, NaN or +inf make the seed or the residual NaN, so the pair is
+    // NaN there without a test (and such lanes take the native path)
+    return fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
 }
 
 // ---------------------------------------------------------------------------
@@ -384,7 +383,7 @@ __device__ __forceinline__ df log_s(float s, df x) {
     const int i = rint_i(__fmaf_rn(m, 1024.0f, -1024.0f)) + AG_LOG_TAB_OFF;   // (m - 1) 1024, exact
     const f4 cl = ld4(kLogCL, i);
     const float c = cl.x;
-    const float A = __fmul_rn(c, p2f(-e));         // c 2^-e, exact
+    const float A = __int_as_float((int)((unsigned)__float_as_int(c) - ((unsigned)e << 23)));   // c 2^-e, exact for valid e
     // x A = p + (x.lo A + p.lo), the pair left unnormalised for the sum
     const df p = two_prod(x.hi, A);
     const float pl = __fmaf_rn(x.lo, A, p.lo);
@@ -404,8 +403,9 @@ __device__ __forceinline__ df log_s(float s, df x) {
         t = fast_two_sum(u.hi, __fadd_rn(__fadd_rn(B.lo, pl), u.lo));
     }
     const df L = mk(cl.y, cl.z);
-    // e ln2 from a table (the index is clamped; out-of-range e is flagged below)
-    const int ei = (e < -127 ? -127 : (e > 128 ? 128 : e)) + AG_LN2_TAB_OFF;
+    // e ln2 from a table covering every e the bits above can give (out-of-range
+    // e is flagged below)
+    const int ei = e + AG_LN2_TAB_OFF;
 #ifdef __CUDA_ARCH__
     const float2 ep = __ldg(reinterpret_cast<const float2*>(kLn2Mul) + ei);
     const df E = mk(ep.x, ep.y);
@@ -627,7 +627,10 @@ __device__ __forceinline__ df dfc(double x) {   // any double (runtime scalars, 
     const float l = isfinite(h) ? __double2float_rn(x - (double)h) : 0.0f;
     return mk(h, l);
 }
-__device__ __forceinline__ df abs_(df x) { return x.hi < 0.0f ? neg(x) : x; }
+// |x|: |hi|, and lo with the sign of hi taken off
+__device__ __forceinline__ df abs_(df x) {
+    return mk(fabsf(x.hi), __int_as_float(__float_as_int(x.lo) ^ (__float_as_int(x.hi) & (int)0x80000000)));
+}
 __device__ __forceinline__ df sign_(df x) {
     return mk(x.hi > 0.0f ? 1.0f : (x.hi < 0.0f ? -1.0f : 0.0f), 0.0f);
 }

@@ -90,10 +90,13 @@ def main():
     out.append("__device__ __align__(16) const float kLogCL[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
     ln2 = mp.log(2)
     # e ln2 for e in [-127, 128] as a float pair (the exponent part of a log)
-    e_hi, e_lo = zip(*[split2(e * ln2) for e in range(-127, 129)])
-    out.append("#define AG_LN2_TAB_OFF 127")
+    # e in [-129, 130]: every exponent the reduction can produce from a float's
+    # bits (including NaN and infinity, +1 for the m >= 1.5 step), so the
+    # index needs no clamp
+    e_hi, e_lo = zip(*[split2(e * ln2) for e in range(-129, 131)])
+    out.append("#define AG_LN2_TAB_OFF 129")
     e_pairs = [v for pair in zip(e_hi, e_lo) for v in pair]
-    out.append("__device__ __align__(8) const float kLn2Mul[512] = {%s};" % ", ".join(fl(v) for v in e_pairs))
+    out.append("__device__ __align__(8) const float kLn2Mul[%d] = {%s};" % (len(e_pairs), ", ".join(fl(v) for v in e_pairs)))
 
     # --- sin/cos at j/2048, j in [-1664, 1664], packed (S hi, S lo, C hi, C lo) --
     # so one 16-byte load serves a lookup; |r - j/2048| <= 2^-12 leaves the
