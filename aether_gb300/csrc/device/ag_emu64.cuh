@@ -356,11 +356,16 @@ __device__ __forceinline__ df exp_(df x) {
 // log(1+t) for |t| <= 2^-10.6: t - t^2/2 in double-float, the rest
 // t^2 (t/3 - t^2/4 + t^3/5) in float (at most 2^-47.6 relative to t).
 __device__ __forceinline__ df log1p_poly(df t) {
-    const df t2 = sqr(t);
+    // h = -t^2/2 as an unnormalised pair: -t.hi^2/2 rounded, its exact error
+    // and -t.hi t.lo; r = t^2 q = (hh + hl) (-2 q), the -2 folded into q (r
+    // needs t^2 to float accuracy, so the t.lo part of h joins it)
     const float th = t.hi;
-    const float q = __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, 0.2f, -0.25f), 0.333333333f));
-    const df s = add_quick(t, scale(t2, -0.5f));
-    return add_quick(s, __fmul_rn(t2.hi, q));
+    const float u = __fmul_rn(-0.5f, th);   // exact
+    const float hh = __fmul_rn(th, u);
+    const float hl = __fmaf_rn(-th, t.lo, __fmaf_rn(th, u, -hh));
+    const float r = __fmul_rn(__fadd_rn(hh, hl),
+                              __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, -0.4f, 0.5f), -0.666666667f)));
+    return add_quick(add_quick(t, mk(hh, hl)), r);
 }
 // log_s(s, x) for s + x > 0 with 2^-120 < s + x < 2^120 known in advance
 // (checked = false) skips the validity test. MODE selects how the reduced
@@ -425,7 +430,8 @@ __device__ __forceinline__ df log_s(float s, df x) {
         const float uu = __fmul_rn(-0.5f, th);
         const float hh = __fmul_rn(th, uu);
         const float hl = __fmaf_rn(-th, t.lo, __fmaf_rn(th, uu, -hh));
-        const float r = __fmul_rn(hh, __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, -0.4f, 0.5f), -0.666666667f)));
+        const float r = __fmul_rn(__fadd_rn(hh, hl),
+                                  __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, -0.4f, 0.5f), -0.666666667f)));
         const df a1 = fast_two_sum(E.hi, L.hi);
         const df a2 = fast_two_sum(a1.hi, th);
         const df a3 = fast_two_sum(a2.hi, hh);   // |h| <= 2^-11.6 |t|
