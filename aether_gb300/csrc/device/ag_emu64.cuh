@@ -11,10 +11,12 @@
 //
 // Accuracy: relative error about 2^-46 per function (a few tens of double
 // ulps in the worst case), against 2^-53 for the native pipe. Samples whose
-// inputs leave [2^-60, 2^60] in magnitude, whose trig arguments exceed
-// 4096*pi/2, or whose outputs are not finite normal values above 2^-90 are
-// recomputed by the generated code with native FP64 (the fallback path), so
-// range, special values and large-argument reduction keep FP64 semantics.
+// inputs leave [2^-50, 2^60] in magnitude, whose products or quotients fall
+// below 2^-102 (where the pair's error terms would be subnormal), whose exp
+// arguments leave (-70, 87), whose trig arguments reach 2^24, or whose
+// outputs are not finite normal values above 2^-90 are recomputed by the
+// generated code with native FP64 (the fallback path), so range, special
+// values and large-argument reduction keep FP64 semantics.
 //
 // Methods (all from the published literature, constants computed by
 // gen_emu64_tables.py): Knuth two-sum, Dekker fast-two-sum, FMA two-product;
@@ -140,6 +142,14 @@ __device__ __forceinline__ df sqr_u(df x) {
     const df c = two_prod(x.hi, x.hi);
     return mk(c.hi, __fmaf_rn(2.0f * x.hi, x.lo, c.lo));
 }
+// Products and quotients below 2^-102 in magnitude: the exact error terms
+// of the pair arithmetic would be subnormal, so the pair loses precision.
+// The lane is flagged for the native path instead.
+#define AG_DF_MIN 1.9721522630525295e-31f   // 2^-102
+__device__ __forceinline__ df ck(df v, bool& ok) {
+    ok = ok && fabsf(v.hi) >= AG_DF_MIN;
+    return v;
+}
 // Scale by an exact power of two.
 __device__ __forceinline__ df scale(df x, float p2) { return mk(__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2)); }
 // Sum where the first term dominates: |x.hi| >= |y.hi| (or x == 0), so the
@@ -213,21 +223,23 @@ __device__ __forceinline__ bool ne(df a, df b) { return !eq(a, b); }
 // ---------------------------------------------------------------------------
 // double <-> double-float, with integer operations only (no F2F).
 // ---------------------------------------------------------------------------
-// |x| in [2^-60, 2^60]: the range where products of a few operands stay
-// normal floats.
+// |x| in [2^-50, 2^60]: the input range of the double-float path. Squares and
+// products of two inputs then stay within [2^-100, 2^120], where the exact
+// error terms of the pair arithmetic are still normal floats (the generator
+// checks every product it cannot prove to stay above 2^-102).
 __device__ __forceinline__ bool in_range(double x) {
     const unsigned ah = (unsigned)__double2hiint(x) & 0x7fffffffu;
-    return ah - (963u << 20) <= (121u << 20) - 1u;
+    return ah - (973u << 20) <= (111u << 20) - 1u;
 }
 // The split of a double, and its range test (the flag is cleared when |x|
-// leaves [2^-60, 2^60]) from the same integer work: the float exponent of the
+// leaves [2^-50, 2^60]) from the same integer work: the float exponent of the
 // head is the double's less 896, the tail's scale 2^(e-1075) is the head's
 // exponent field less 52 (with the sign carried along).
 __device__ __forceinline__ df from_double_ck(double x, bool& ok) {
     const unsigned h32 = (unsigned)__double2hiint(x);
     const unsigned l32 = (unsigned)__double2loint(x);
     const unsigned t = (h32 & 0x7fffffffu) - (896u << 20);
-    ok = ok && t - (67u << 20) <= (121u << 20) - 1u;
+    ok = ok && t - (77u << 20) <= (111u << 20) - 1u;
     // hi: the top 24 significant bits (truncated), re-biased to float
     const unsigned hb = __funnelshift_l(l32, t, 3) | (h32 & 0x80000000u);
     // lo: the remaining 29 bits, rounded to a float and scaled by +-2^(ex-1075);
@@ -325,7 +337,10 @@ __device__ __forceinline__ df rsqrt_(df x) {
 // ---------------------------------------------------------------------------
 // exp: x = (64k + j) ln2/64 + r, |r| <= ln2/128; e^x = 2^k 2^(j/64) e^r.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ df exp_(df x) {
+// The flag is cleared outside -70 < x < 87, where 2^k leaves the float range
+// or the result's low part would be subnormal (the native lane computes it).
+__device__ __forceinline__ df exp_(df x, bool& ok) {
+    ok = ok && x.hi > -70.0f && x.hi < 87.0f;
     const float mf = rint_f(__fmul_rn(x.hi, AG_INV_LN2_64));
     const int m = rint_i(__fmul_rn(x.hi, AG_INV_LN2_64));
     const float r1 = __fmaf_rn(-mf, AG_LN2_64_1, x.hi);   // exact (Sterbenz)

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <cmath>
 #include <set>
 #include <sstream>
 #include <stdexcept>
@@ -407,6 +408,12 @@ struct Gen {
     std::string pre = "t";    // variable prefix
     bool direct = false;      // leaves load their own sample `s` (per-lane fallback function)
     std::vector<signed char> nn_memo;
+    // Double-float magnitude bounds: floor(log2 |v|) of every non-zero value of
+    // node id lies in [elo, ehi] (wide open when unknown). A product whose
+    // bounds cannot go below 2^-102 needs no range check (ag::e64::ck).
+    static constexpr int kOpenLo = -100000, kOpenHi = 100000, kSafeLo = -101;
+    std::vector<int> elo, ehi;
+    std::string cur_ok = "ok_";   // the range flag of the node being emitted
 
     // Conservative sign analysis: true when node `id` can never be negative,
     // which lets emulated sums skip the cancellation-safe form.
@@ -443,11 +450,21 @@ struct Gen {
         const Node& n = P.nodes[size_t(id)];
         return dfm && n.op == "in" && n.dtype == DType::F32;
     }
-    // `u`: the product is read only by sums and may stay unnormalised
+    // `u`: the product is read only by sums and may stay unnormalised. The
+    // range check is left out when the factors' bounds keep it above 2^-102.
     std::string mulx(bool u, int ia, int ib, const std::string& a, const std::string& b) {
-        if (exact_f32(ia) && exact_f32(ib)) return "ag::e64::two_prod(" + a + ".hi, " + b + ".hi)";
-        if (dfm && ia == ib && a == b) return sqr(u, a);   // x*x: the square's cheaper form
-        return mul(a, b);
+        const bool safe = lo_of(ia) + lo_of(ib) >= kSafeLo;
+        if (exact_f32(ia) && exact_f32(ib)) {
+            const std::string p = "ag::e64::two_prod(" + a + ".hi, " + b + ".hi)";
+            return checked(p, safe);
+        }
+        if (dfm && ia == ib && a == b) return checked(sqr(u, a), safe);   // x*x: the square's cheaper form
+        return dfm ? checked("ag::e64::mul(" + a + ", " + b + ")", safe) : mul(a, b);
+    }
+    int lo_of(int id) const { return elo.empty() ? kOpenLo : elo[size_t(id)]; }
+    int hi_of(int id) const { return ehi.empty() ? kOpenHi : ehi[size_t(id)]; }
+    std::string checked(const std::string& v, bool safe) const {
+        return safe ? v : "ag::e64::ck(" + v + ", " + cur_ok + ")";
     }
     // Nodes read only by sums (add, sub): a square feeding them may stay an
     // unnormalised pair, saving its final Fast2Sum. The root of an emulated
@@ -475,12 +492,16 @@ struct Gen {
         if (dfm) return "ag::e64::sub(" + a + ", " + b + ")";
         return L.contract ? "(" + a + " - " + b + ")" : "ag::rn_sub(" + a + ", " + b + ")";
     }
+    // Products and quotients inside composite nodes carry the range check
+    // (a product with a literal zero is exact and needs none).
+    std::set<std::string> zero_vars;
     std::string mul(const std::string& a, const std::string& b) const {
-        if (dfm) return "ag::e64::mul(" + a + ", " + b + ")";
+        if (dfm && (zero_vars.count(a) || zero_vars.count(b))) return "ag::e64::mul(" + a + ", " + b + ")";
+        if (dfm) return "ag::e64::ck(ag::e64::mul(" + a + ", " + b + "), " + cur_ok + ")";
         return L.contract ? "(" + a + " * " + b + ")" : "ag::rn_mul(" + a + ", " + b + ")";
     }
     std::string div(const std::string& a, const std::string& b) const {
-        if (dfm) return "ag::e64::div(" + a + ", " + b + ")";
+        if (dfm) return "ag::e64::ck(ag::e64::div(" + a + ", " + b + "), " + cur_ok + ")";
         return "ag::rn_div(" + a + ", " + b + ")";
     }
     std::string neg(const std::string& a) const { return dfm ? "ag::e64::neg(" + a + ")" : "(-" + a + ")"; }
@@ -500,8 +521,8 @@ struct Gen {
         std::string a;
         for (size_t i = 0; i < args.size(); ++i) a += (i ? ", " : "") + args[i];
         if (!dfm) return "ag::f_" + name + "(" + a + ")";
-        static const std::set<std::string> own = {"sqrt", "rsqrt", "exp", "log", "log1p", "abs", "sign", "min", "max"};
-        if (name == "sin" || name == "cos") return "ag::e64::" + name + "_(" + a + ", " + okv(id) + ")";
+        static const std::set<std::string> own = {"sqrt", "rsqrt", "log", "log1p", "abs", "sign", "min", "max"};
+        if (name == "sin" || name == "cos" || name == "exp") return "ag::e64::" + name + "_(" + a + ", " + okv(id) + ")";
         if (name == "log1p" && abs_of_input(P.nodes[size_t(id)].kids[0]))
             return "ag::e64::log1p_nn_(" + a + ")";   // |input| is >= 0 and within the input range check
         if (own.count(name)) return "ag::e64::" + name + "_(" + a + ")";
@@ -525,6 +546,59 @@ struct Gen {
         val[size_t(id)] = names;
     }
 
+    // Magnitude bounds of node id from its kids' (conservative; open when
+    // nothing better is known). Inputs of the double-float path are range
+    // checked to [2^-50, 2^60]; exact f32 inputs are not checked.
+    void bounds(int id) {
+        if (!dfm) return;
+        if (elo.empty()) {
+            elo.assign(P.nodes.size(), kOpenLo);
+            ehi.assign(P.nodes.size(), kOpenHi);
+        }
+        const Node& n = P.nodes[size_t(id)];
+        const std::string& op = n.op;
+        auto L = [&](int j) { return elo[size_t(n.kids[size_t(j)])]; };
+        auto H = [&](int j) { return ehi[size_t(n.kids[size_t(j)])]; };
+        auto clampb = [](int v) { return v < kOpenLo ? kOpenLo : (v > kOpenHi ? kOpenHi : v); };
+        int lo = kOpenLo, hi = kOpenHi;
+        if (op == "in") {
+            if (n.dtype == DType::F64) lo = -50, hi = 60;
+            else if (n.dtype == DType::F32) lo = -149, hi = 127;
+        } else if (op == "lit") {
+            if (n.lit != 0.0 && std::isfinite(n.lit)) {
+                lo = hi = std::ilogb(n.lit);
+            } else if (n.lit == 0.0) {
+                lo = kOpenHi, hi = kOpenLo;   // an exact zero: products with it are exact
+            }
+        } else if (op == "neg" || op == "abs" || op == "bcast" || op == "at0" || op == "comp" || op == "seg" ||
+                   op == "row" || op == "col" || op == "transpose" || op == "block" || op == "reshape" ||
+                   op == "stack") {
+            lo = kOpenHi, hi = kOpenLo;
+            for (size_t j = 0; j < n.kids.size(); ++j) {
+                lo = std::min(lo, L(int(j)));
+                hi = std::max(hi, H(int(j)));
+            }
+        } else if (op == "sq") {
+            lo = clampb(2 * L(0)), hi = clampb(2 * H(0) + 1);
+        } else if (op == "mul") {
+            lo = clampb(L(0) + L(1)), hi = clampb(H(0) + H(1) + 1);
+        } else if (op == "sqrt") {
+            lo = L(0) <= kOpenLo ? kOpenLo : L(0) / 2 - 1, hi = H(0) >= kOpenHi ? kOpenHi : H(0) / 2 + 1;
+        } else if (op == "rsqrt") {
+            lo = H(0) >= kOpenHi ? kOpenLo : -(H(0) / 2) - 2, hi = L(0) <= kOpenLo ? kOpenHi : -(L(0) / 2) + 2;
+        } else if (op == "add" && nonneg(n.kids[0]) && nonneg(n.kids[1])) {
+            // no cancellation; an exact zero (an empty interval) adds nothing
+            const bool z0 = L(0) > H(0), z1 = L(1) > H(1);
+            lo = z0 ? L(1) : (z1 ? L(0) : std::max(L(0), L(1)));
+            hi = clampb(std::max(H(0), H(1)) + 1);
+        } else if (op == "log1p" && nonneg(n.kids[0])) {
+            lo = L(0) <= kOpenLo ? kOpenLo : std::min(L(0) - 1, -1);   // log1p(y) >= min(y, 1)/2
+            hi = H(0) <= 0 ? H(0) : 7;
+        }
+        elo[size_t(id)] = lo;
+        ehi[size_t(id)] = hi;
+    }
+
     const std::vector<std::string>& emit(int id) {
         if (done[size_t(id)]) return val[size_t(id)];
         const Node& n = P.nodes[size_t(id)];
@@ -533,6 +607,7 @@ struct Gen {
         auto K = [&](int j) -> const Node& { return P.nodes[size_t(n.kids[size_t(j)])]; };
         const std::string& op = n.op;
         const bool c0 = ctx[size_t(id)] != 0;
+        cur_ok = okv(id);
         std::vector<std::string> e;
         const std::string gid = c0 ? "g0" : "g";
         const std::string sid = pre + std::to_string(id);
@@ -562,6 +637,7 @@ struct Gen {
             def(id, {dfm ? "ag::e64::mk(a.sch[" + k + "], a.scl[" + k + "])" : "(" + W + ")" + s});
         } else if (op == "lit") {
             def(id, {lit(n.lit)});
+            if (n.lit == 0.0) zero_vars.insert(val[size_t(id)][0]);   // products with it are exact zeros
         } else if (op == "bcast") {
             for (int c = 0; c < n.comps; ++c) e.push_back(V(0)[0]);
             val[size_t(id)] = e;   // aliases: no new variables
@@ -572,7 +648,7 @@ struct Gen {
         } else if (unary_ops().count(op)) {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x = V(0)[size_t(c)];
-                if (op == "sq") e.push_back(dfm ? sqr(sum_only(id), x) : mul(x, x));
+                if (op == "sq") e.push_back(dfm ? checked(sqr(sum_only(id), x), 2 * lo_of(n.kids[0]) >= kSafeLo) : mul(x, x));
                 else if (op == "sqrt" && dfm && nonneg(n.kids[0])) e.push_back("ag::e64::sqrt_nn_(" + x + ")");
                 else if (op == "neg") e.push_back(neg(x));
                 else e.push_back(call(op, {x}, id));
@@ -808,6 +884,7 @@ struct Gen {
         } else {
             fail("no generator for '" + op + "'");
         }
+        bounds(id);
         done[size_t(id)] = 1;
         return val[size_t(id)];
     }

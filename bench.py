@@ -574,17 +574,24 @@ def run_ours(args):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
+        # Three timed runs of e_steps back-to-back steps each; the median run
+        # is reported (the host link is shared with the machine's other GPUs),
+        # every run beside it.
         e_steps = max(3, min(args.steps, 6))
-        t0 = time.perf_counter()
-        for _ in range(e_steps):
-            e2e_step()
-        ag._abi.check(L.aether_stream_sync(local, down_p))
-        e_ms = (time.perf_counter() - t0) * 1e3 / e_steps
+        runs = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            for _ in range(e_steps):
+                e2e_step()
+            ag._abi.check(L.aether_stream_sync(local, down_p))
+            runs.append((time.perf_counter() - t0) * 1e3 / e_steps)
+        e_ms = statistics.median(runs)
         e_ms = shard.max_over_ranks(e_ms, group=dist.group.WORLD if dist else None)
         e2e = {"value": round(ws * (BYTES_EXPR + BYTES_FILL) / (e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
                "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3),
                "pipeline": "%d sample blocks: upload, compute and download streams; %d steps back to back, "
-                           "one synchronisation after the last" % (len(chunks), e_steps)}
+                           "one synchronisation after the last; median of 3 runs" % (len(chunks), e_steps),
+               "ms_per_step_runs": [round(r, 3) for r in runs]}
         # The host link measured in the same process: one large copy each
         # way, then both at once; the copy time of one step at those rates
         # is the bound the end-to-end number is read against.
