@@ -549,6 +549,7 @@ struct Gen {
     // Magnitude bounds of node id from its kids' (conservative; open when
     // nothing better is known). Inputs of the double-float path are range
     // checked to [2^-50, 2^60]; exact f32 inputs are not checked.
+    static int floordiv(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
     void bounds(int id) {
         if (!dfm) return;
         if (elo.empty()) {
@@ -582,10 +583,10 @@ struct Gen {
             lo = clampb(2 * L(0)), hi = clampb(2 * H(0) + 1);
         } else if (op == "mul") {
             lo = clampb(L(0) + L(1)), hi = clampb(H(0) + H(1) + 1);
-        } else if (op == "sqrt") {
-            lo = L(0) <= kOpenLo ? kOpenLo : L(0) / 2 - 1, hi = H(0) >= kOpenHi ? kOpenHi : H(0) / 2 + 1;
-        } else if (op == "rsqrt") {
-            lo = H(0) >= kOpenHi ? kOpenLo : -(H(0) / 2) - 2, hi = L(0) <= kOpenLo ? kOpenHi : -(L(0) / 2) + 2;
+        } else if (op == "sqrt") {   // 2^L <= x < 2^(H+1): 2^(L/2) <= sqrt x < 2^((H+1)/2)
+            lo = L(0) <= kOpenLo ? kOpenLo : floordiv(L(0), 2), hi = H(0) >= kOpenHi ? kOpenHi : floordiv(H(0), 2) + 1;
+        } else if (op == "rsqrt") {   // 2^(-(H+1)/2) < 1/sqrt x <= 2^(-L/2)
+            lo = H(0) >= kOpenHi ? kOpenLo : floordiv(-(H(0) + 1), 2), hi = L(0) <= kOpenLo ? kOpenHi : floordiv(-L(0), 2);
         } else if (op == "add" && nonneg(n.kids[0]) && nonneg(n.kids[1])) {
             // no cancellation; an exact zero (an empty interval) adds nothing
             const bool z0 = L(0) > H(0), z1 = L(1) > H(1);

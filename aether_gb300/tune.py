@@ -1,9 +1,11 @@
 """Autotuner: choose block shape, lane groups per thread, vector width and
 occupancy bound per plan, by timing candidate lowerings on the device.
 
-Results are cached in a JSON file keyed by the plan text, the math mode and
-the device name ($AETHER_GB300_TUNE_CACHE, else ~/.cache/aether_gb300/
-tune.json), so a plan is tuned once per device and later processes reuse the
+Results are cached in a JSON file keyed by the plan text, the math mode, the
+device name, the digest of the device headers every kernel includes and the
+digest of the kernel text the generator writes for the plan
+($AETHER_GB300_TUNE_CACHE, else ~/.cache/aether_gb300/tune.json), so a plan
+is tuned once per device and code version and later processes reuse the
 winner. Candidates are valid by construction (block a multiple of 32 up to
 1024, vec in {1, 2, 4}, ipt in {1, 2, 4}); a candidate that fails to compile
 or launch is skipped, never retried.
@@ -46,8 +48,21 @@ def _code_digest():
     return "%016x" % _abi.lib().aether_rtc_digest()
 
 
+def _generated_digest(ir, math, contract):
+    """Digest of the kernel text the generator writes for this plan (at the
+    default lowering): a tuning result also goes stale when the generator
+    changes what it emits."""
+    from . import _abi
+    try:
+        src = _abi.generate(ir, _abi.lowering(math=math, contract=contract))
+    except Exception:
+        return "-"
+    return hashlib.sha1(src.encode()).hexdigest()[:16]
+
+
 def _key(ir, math, contract):
-    h = hashlib.sha1(("%s|%d|%d|%s|%s" % (ir, math, contract, _device_name(), _code_digest())).encode()).hexdigest()
+    h = hashlib.sha1(("%s|%d|%d|%s|%s|%s" % (ir, math, contract, _device_name(), _code_digest(),
+                                             _generated_digest(ir, math, contract))).encode()).hexdigest()
     return h
 
 

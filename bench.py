@@ -199,6 +199,20 @@ def link_rates(L, dev, h_in, a_in, h_out, a_out, nbytes, s_up, s_down):
             "both_gbs": round(one(True, True), 1), "bytes_each_way": nbytes}
 
 
+def h2d_probe(L, dev, h_in, a_in, nbytes, s_up):
+    """One host->device copy of nbytes, timed with events on the upload stream (GB/s)."""
+    import ctypes
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s_up)
+    ag_check(L.aether_copy(1, dev, ctypes.c_void_p(a_in.data.data_ptr()), 2, 0, ctypes.c_void_p(h_in.data_ptr()),
+                           nbytes, ctypes.c_void_p(s_up.cuda_stream)))
+    e1.record(s_up)
+    e1.synchronize()
+    return nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
 def ag_check(rc):
     from aether_gb300 import _abi
     _abi.check(rc)
@@ -577,9 +591,12 @@ def run_ours(args):
         # Three timed runs of e_steps back-to-back steps each; the median run
         # is reported (the host link is shared with the machine's other GPUs),
         # every run beside it.
+        # Each run is preceded by a one-copy probe of the host->device rate,
+        # so a slow run can be told from a busy link.
         e_steps = max(3, min(args.steps, 6))
-        runs = []
+        runs, probes = [], []
         for _ in range(3):
+            probes.append(h2d_probe(L, local, host_in[0], arrs[0], nb // 4, s_up))
             t0 = time.perf_counter()
             for _ in range(e_steps):
                 e2e_step()
@@ -591,7 +608,8 @@ def run_ours(args):
                "h2d_bytes_per_step": 4 * nb, "d2h_bytes_per_step": nb + N_FILL * 8, "ms_per_step": round(e_ms, 3),
                "pipeline": "%d sample blocks: upload, compute and download streams; %d steps back to back, "
                            "one synchronisation after the last; median of 3 runs" % (len(chunks), e_steps),
-               "ms_per_step_runs": [round(r, 3) for r in runs]}
+               "ms_per_step_runs": [round(r, 3) for r in runs],
+               "h2d_gbs_before_runs": [round(p, 1) for p in probes]}
         # The host link measured in the same process: one large copy each
         # way, then both at once; the copy time of one step at those rates
         # is the bound the end-to-end number is read against.

@@ -121,6 +121,34 @@ def test_structural_cse_shares_subtrees():
     assert src.count("ag::f_sin(") == 3   # once per component, not twice
 
 
+def _fast_path(src):
+    """The double-float lane loop of a generated source (without the native
+    recomputation function)."""
+    return src[src.index("ag_chunk"):]
+
+
+def test_emulated_products_are_range_checked_only_where_bounds_need_it():
+    # inputs of the double-float path lie in [2^-50, 2^60]: a*a + b*b, the
+    # square root and log1p of |c| keep every product above 2^-102, so the
+    # config-2a tree carries no product check; a product of three inputs
+    # can reach 2^-150 and is checked; exp carries its own range flag
+    a, b, c, d0 = (_leaf(k) for k in range(4))
+    cfg2a = (ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c))
+             + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0))
+    src = _fast_path(_abi.generate(plan_text("f64", (3,), "set", cfg2a, IrContext()), _abi.lowering(math=1)))
+    assert "ag::e64::ck(" not in src
+    assert src.count("ag::e64::from_double_ck(") == 12
+    src = _fast_path(_abi.generate(plan_text("f64", (3,), "set", (a * b) * c, IrContext()), _abi.lowering(math=1)))
+    assert src.count("ag::e64::ck(") == 3          # the outer product, once per component
+    src = _fast_path(_abi.generate(plan_text("f64", (3,), "set", ag.cwiseExp(a) * b, IrContext()),
+                                   _abi.lowering(math=1)))
+    assert src.count("ag::e64::exp_(") == 3 and src.count(", ok_)") >= 6
+    # exact f32 operands are not range checked, so their products are
+    x, y = _leaf(7, (8,), "f32"), _leaf(8, (8,), "f32")
+    src = _fast_path(_abi.generate(plan_text("f32", (8,), "set", x * y, IrContext()), _abi.lowering(math=2)))
+    assert src.count("ag::e64::ck(ag::e64::two_prod(") == 8
+
+
 def test_emulated_math_requires_f64_plan():
     a = _leaf(0, (3,), "f32")
     ir = plan_text("f32", (3,), "set", a + a, IrContext())
