@@ -495,6 +495,13 @@ struct Gen {
     // Products and quotients inside composite nodes carry the range check
     // (a product with a literal zero is exact and needs none).
     std::set<std::string> zero_vars;
+    // Products of two kid values of the node being emitted, unchecked when
+    // the kids' bounds keep every such product above 2^-102.
+    bool kids_safe = false;
+    std::string mulkk(const std::string& a, const std::string& b) const {
+        if (dfm && kids_safe) return "ag::e64::mul(" + a + ", " + b + ")";
+        return mul(a, b);
+    }
     std::string mul(const std::string& a, const std::string& b) const {
         if (dfm && (zero_vars.count(a) || zero_vars.count(b))) return "ag::e64::mul(" + a + ", " + b + ")";
         if (dfm) return "ag::e64::ck(ag::e64::mul(" + a + ", " + b + "), " + cur_ok + ")";
@@ -609,6 +616,12 @@ struct Gen {
         const std::string& op = n.op;
         const bool c0 = ctx[size_t(id)] != 0;
         cur_ok = okv(id);
+        kids_safe = false;
+        if (dfm && !n.kids.empty()) {
+            int m = kOpenHi;
+            for (int k : n.kids) m = std::min(m, lo_of(k));
+            kids_safe = m > kOpenLo && 2 * m >= kSafeLo;
+        }
         std::vector<std::string> e;
         const std::string gid = c0 ? "g0" : "g";
         const std::string sid = pre + std::to_string(id);
@@ -726,8 +739,8 @@ struct Gen {
         } else if (op == "cross") {   // expr/nodes/Geometric.h:55-72
             const auto& l = V(0);
             const auto& r = V(1);
-            e = {sub(mul(l[1], r[2]), mul(l[2], r[1])), sub(mul(l[2], r[0]), mul(l[0], r[2])),
-                 sub(mul(l[0], r[1]), mul(l[1], r[0]))};
+            e = {sub(mulkk(l[1], r[2]), mulkk(l[2], r[1])), sub(mulkk(l[2], r[0]), mulkk(l[0], r[2])),
+                 sub(mulkk(l[0], r[1]), mulkk(l[1], r[0]))};
             def(id, e);
         } else if (op == "unit") {   // Geometric.h:99-103 on a per-sample (Item) value
             const auto& a = V(0);
@@ -740,10 +753,10 @@ struct Gen {
         } else if (op == "qmul") {   // expr/nodes/Quaternion.h:60-79
             const auto& l = V(0);
             const auto& r = V(1);
-            e = {sub(sub(sub(mul(l[0], r[0]), mul(l[1], r[1])), mul(l[2], r[2])), mul(l[3], r[3])),
-                 sub(add(add(mul(l[0], r[1]), mul(l[1], r[0])), mul(l[2], r[3])), mul(l[3], r[2])),
-                 add(add(sub(mul(l[0], r[2]), mul(l[1], r[3])), mul(l[2], r[0])), mul(l[3], r[1])),
-                 add(sub(add(mul(l[0], r[3]), mul(l[1], r[2])), mul(l[2], r[1])), mul(l[3], r[0]))};
+            e = {sub(sub(sub(mulkk(l[0], r[0]), mulkk(l[1], r[1])), mulkk(l[2], r[2])), mulkk(l[3], r[3])),
+                 sub(add(add(mulkk(l[0], r[1]), mulkk(l[1], r[0])), mulkk(l[2], r[3])), mulkk(l[3], r[2])),
+                 add(add(sub(mulkk(l[0], r[2]), mulkk(l[1], r[3])), mulkk(l[2], r[0])), mulkk(l[3], r[1])),
+                 add(sub(add(mulkk(l[0], r[3]), mulkk(l[1], r[2])), mulkk(l[2], r[1])), mulkk(l[3], r[0]))};
             def(id, e);
         } else if (op == "qconj") {   // Quaternion.h:103-108
             const auto& a = V(0);
@@ -755,9 +768,9 @@ struct Gen {
             const std::string t = sid + "q";
             std::ostringstream& o = out_for(id);
             const std::string two = lit(2.0);
-            o << "        const " << W << " " << t << "x = " << mul(two, sub(mul(q[2], v[2]), mul(q[3], v[1]))) << ";\n";
-            o << "        const " << W << " " << t << "y = " << mul(two, sub(mul(q[3], v[0]), mul(q[1], v[2]))) << ";\n";
-            o << "        const " << W << " " << t << "z = " << mul(two, sub(mul(q[1], v[1]), mul(q[2], v[0]))) << ";\n";
+            o << "        const " << W << " " << t << "x = " << mul(two, sub(mulkk(q[2], v[2]), mulkk(q[3], v[1]))) << ";\n";
+            o << "        const " << W << " " << t << "y = " << mul(two, sub(mulkk(q[3], v[0]), mulkk(q[1], v[2]))) << ";\n";
+            o << "        const " << W << " " << t << "z = " << mul(two, sub(mulkk(q[1], v[1]), mulkk(q[2], v[0]))) << ";\n";
             e = {add(add(v[0], mul(q[0], t + "x")), sub(mul(q[2], t + "z"), mul(q[3], t + "y"))),
                  add(add(v[1], mul(q[0], t + "y")), sub(mul(q[3], t + "x"), mul(q[1], t + "z"))),
                  add(add(v[2], mul(q[0], t + "z")), sub(mul(q[1], t + "y"), mul(q[2], t + "x")))};
@@ -775,7 +788,7 @@ struct Gen {
             const std::string rd = sid + "rdet";
             auto q = [&](const std::string& num) { return dfm ? mul(num, rd) : div(num, d); };
             if (dim == 2) {
-                o << "        const " << W << " " << d << " = " << sub(mul(m[0], m[3]), mul(m[1], m[2])) << ";\n";
+                o << "        const " << W << " " << d << " = " << sub(mulkk(m[0], m[3]), mulkk(m[1], m[2])) << ";\n";
                 if (dfm && op == "inv") o << "        const " << W << " " << rd << " = ag::e64::recip(" << d << ");\n";
                 if (op == "det") e = {d};
                 else e = {q(m[3]), q(neg(m[1])), q(neg(m[2])), q(m[0])};
@@ -783,16 +796,16 @@ struct Gen {
                 const std::string &a = m[0], &b = m[1], &c = m[2], &dd = m[3], &ee = m[4], &f = m[5], &g = m[6],
                                   &h = m[7], &k = m[8];
                 o << "        const " << W << " " << d << " = "
-                  << add(sub(mul(a, sub(mul(ee, k), mul(f, h))), mul(b, sub(mul(dd, k), mul(f, g)))),
-                         mul(c, sub(mul(dd, h), mul(ee, g))))
+                  << add(sub(mul(a, sub(mulkk(ee, k), mulkk(f, h))), mul(b, sub(mulkk(dd, k), mulkk(f, g)))),
+                         mul(c, sub(mulkk(dd, h), mulkk(ee, g))))
                   << ";\n";
                 if (dfm && op == "inv") o << "        const " << W << " " << rd << " = ag::e64::recip(" << d << ");\n";
                 if (op == "det") {
                     e = {d};
                 } else {
-                    e = {q(sub(mul(ee, k), mul(f, h))), q(sub(mul(c, h), mul(b, k))), q(sub(mul(b, f), mul(c, ee))),
-                         q(sub(mul(f, g), mul(dd, k))), q(sub(mul(a, k), mul(c, g))), q(sub(mul(c, dd), mul(a, f))),
-                         q(sub(mul(dd, h), mul(ee, g))), q(sub(mul(b, g), mul(a, h))), q(sub(mul(a, ee), mul(b, dd)))};
+                    e = {q(sub(mulkk(ee, k), mulkk(f, h))), q(sub(mulkk(c, h), mulkk(b, k))), q(sub(mulkk(b, f), mulkk(c, ee))),
+                         q(sub(mulkk(f, g), mulkk(dd, k))), q(sub(mulkk(a, k), mulkk(c, g))), q(sub(mulkk(c, dd), mulkk(a, f))),
+                         q(sub(mulkk(dd, h), mulkk(ee, g))), q(sub(mulkk(b, g), mulkk(a, h))), q(sub(mulkk(a, ee), mulkk(b, dd)))};
                 }
             }
             def(id, e);
@@ -809,19 +822,19 @@ struct Gen {
             const auto& sb = K(1).shape;
             if (op == "outer") {
                 for (int i = 0; i < sa[0]; ++i)
-                    for (int j = 0; j < sb[0]; ++j) e.push_back(mul(a[size_t(i)], b[size_t(j)]));
+                    for (int j = 0; j < sb[0]; ++j) e.push_back(mulkk(a[size_t(i)], b[size_t(j)]));
             } else if (op == "matvec") {
                 for (int i = 0; i < sa[0]; ++i) {
-                    std::string acc = mul(a[size_t(i * sa[1])], b[0]);
-                    for (int k = 1; k < sa[1]; ++k) acc = add(mul(a[size_t(i * sa[1] + k)], b[size_t(k)]), acc);
+                    std::string acc = mulkk(a[size_t(i * sa[1])], b[0]);
+                    for (int k = 1; k < sa[1]; ++k) acc = add(mulkk(a[size_t(i * sa[1] + k)], b[size_t(k)]), acc);
                     e.push_back(acc);
                 }
             } else {
                 for (int i = 0; i < sa[0]; ++i)
                     for (int j = 0; j < sb[1]; ++j) {
-                        std::string acc = mul(a[size_t(i * sa[1])], b[size_t(j)]);
+                        std::string acc = mulkk(a[size_t(i * sa[1])], b[size_t(j)]);
                         for (int k = 1; k < sa[1]; ++k)
-                            acc = add(mul(a[size_t(i * sa[1] + k)], b[size_t(k * sb[1] + j)]), acc);
+                            acc = add(mulkk(a[size_t(i * sa[1] + k)], b[size_t(k * sb[1] + j)]), acc);
                         e.push_back(acc);
                     }
             }
@@ -834,7 +847,7 @@ struct Gen {
                 if (op == "dot") return mulx(false, n.kids[0], n.kids[1], a[size_t(c)], V(1)[size_t(c)]);
                 if (op == "sum") return a[size_t(c)];
                 if (op == "maxnorm") return call("abs", {a[size_t(c)]}, id);
-                return mul(a[size_t(c)], a[size_t(c)]);
+                return mulkk(a[size_t(c)], a[size_t(c)]);
             };
             std::string acc = term(0);
             for (int c = 1; c < m; ++c) {
