@@ -278,15 +278,15 @@ __device__ __forceinline__ df from_u64(ag_u64 w) {
     return fast_two_sum(h, l);
 }
 __device__ __forceinline__ float p2f(int k) { return __int_as_float((k + 127) << 23); }   // 2^k, |k| <= 126
-// sgn w 2^-54 for 0 < w < 2^53: normalised so the leading bit sits at 2^52,
-// the top 24 bits exact and the next 29 rounded once (2^-48 relative); the
+// sgn w 2^-54 for 0 < w < 2^54: normalised so the leading bit sits at 2^53,
+// the top 24 bits exact and the next 30 rounded once (2^-48 relative); the
 // pair is left with |lo| < ulp(hi). sgn is the sign bit (0 or 0x80000000).
-__device__ __forceinline__ df from_u53_2m54(ag_u64 w, ag_u32 sgn) {
-    const int lz = __clzll((long long)w) - 11;   // 0 .. 52
-    const ag_u64 wn = w << lz;                    // [2^52, 2^53)
-    const ag_u32 sc = ((ag_u32)(102 - lz) << 23) | sgn;   // +-2^(-25-lz): 2^29 units of wn, times 2^-54
-    const float h = __fmul_rn(__uint2float_rn((ag_u32)(wn >> 29)), __int_as_float(sc));
-    const float l = __fmul_rn(__uint2float_rn((ag_u32)wn & 0x1fffffffu), __int_as_float(sc - (29u << 23)));
+__device__ __forceinline__ df from_u54_2m54(ag_u64 w, ag_u32 sgn) {
+    const int lz = __clzll((long long)w) - 10;   // 0 .. 53
+    const ag_u64 wn = w << lz;                    // [2^53, 2^54)
+    const ag_u32 sc = ((ag_u32)(103 - lz) << 23) | sgn;   // +-2^(-24-lz): 2^30 units of wn, times 2^-54
+    const float h = __fmul_rn(__uint2float_rn((ag_u32)(wn >> 30)), __int_as_float(sc));
+    const float l = __fmul_rn(__uint2float_rn((ag_u32)wn & 0x3fffffffu), __int_as_float(sc - (30u << 23)));
     return mk(h, l);
 }
 // Round to nearest integer for |x| < 2^22 with one FP32 add (no conversion unit).
@@ -614,19 +614,27 @@ __device__ __forceinline__ df draw01_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
 template <bool U = false>
 __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag::q4 x = ag::philox_block(seed, g, c);
+    // u is the reference's double z 2^-53 + 2^-54 (random/detail/Backend.h
+    // uniformDoubleHq): exact below 1/2, rounded to even above it, where it is
+    // k 2^-53 with k = z + (z & 1). So u = w 2^-54 with w = 2 z + 1 below 1/2,
+    // and 1 - u = w 2^-54 with w = 2^54 - 2 k (even, at most 2^53) above it.
     const ag_u64 z = (ag_u64)x.x ^ ((ag_u64)x.y << 21);
     const bool lower = z < (1ull << 52);
-    const ag_u64 w = lower ? 2ull * z + 1ull : 2ull * ((1ull << 53) - 1ull - z) + 1ull;
-    // log(u) for u in [2^-54, 1/2] or log1p(-w) for w in [2^-54, 1/2]: always valid
-    const df L = log_s<false, LOG_SRT>(lower ? 0.0f : 1.0f, from_u53_2m54(w, lower ? 0u : 0x80000000u));
+    const ag_u64 w = lower ? 2ull * z + 1ull : (1ull << 54) - 2ull * (z + (z & 1ull));
+    // log(u) for u in [2^-54, 1/2) or log1p(-w) for w in [0, 1/2]; w = 0 (u
+    // rounded to 1) gives a zero argument to the square root below, whose NaN
+    // sends the lane to the native path
+    const df L = log_s<false, LOG_SRT>(lower ? 0.0f : 1.0f, from_u54_2m54(w, lower ? 0u : 0x80000000u));
     const df sv = sqrt_pos_(scale(L, -2.0f));   // log u < 0: the argument is positive
-    // v = V 2^-53 with V = 2 zy + 1 odd, V < 2^54. In integers: K = round(V /
-    // 2^41) counts steps of 1/4096 half-turn, q = round(K / 2048) is the
-    // quadrant, j = K - 2048 q in [-1024, 1024] the table point pi j/4096,
-    // and R = V - 2^41 K (|R| <= 2^40) the remainder, exact in a double-float:
-    // sin(pi v) keeps full relative accuracy next to the zeros of the sine.
+    // v is the reference's double zy 2^-52 + 2^-53: exact below 1, rounded to
+    // even above it. So v = V 2^-53 with V = 2 zy + 1, or 2 (zy + (zy & 1))
+    // for zy >= 2^52, V <= 2^54. In integers: K = round(V / 2^41) counts steps
+    // of 1/4096 half-turn, q = round(K / 2048) is the quadrant, j = K - 2048 q
+    // in [-1024, 1024] the table point pi j/4096, and R = V - 2^41 K (|R| <=
+    // 2^40) the remainder, exact in a double-float: sin(pi v) keeps full
+    // relative accuracy next to the zeros of the sine.
     const ag_u64 zy = (ag_u64)x.z ^ ((ag_u64)x.w << 21);
-    const ag_u64 V = 2ull * zy + 1ull;
+    const ag_u64 V = zy < (1ull << 52) ? 2ull * zy + 1ull : 2ull * (zy + (zy & 1ull));
     const ag_u32 vh = (ag_u32)(V >> 32), vl = (ag_u32)V;
     const ag_u32 K = (vh + 256u) >> 9;   // (V + 2^40) >> 41
     const int q = (int)((K + 1024u) >> 11);

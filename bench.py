@@ -138,8 +138,8 @@ def cpu_leg(steps, warmup, nthreads=0, expr_samples=1 << 23, fill_samples=1 << 2
     times = []
     for i in range(warmup + steps):
         t0 = time.perf_counter()
-        po.cfg2a(*ins, nthreads=nt)
-        po.fill_normal_f64(key_fill, 0.0, 1.0, 1, fill_samples, nthreads=nt)
+        d_out = po.cfg2a(*ins, nthreads=nt)
+        z_out = po.fill_normal_f64(key_fill, 0.0, 1.0, 1, fill_samples, nthreads=nt)
         dt = time.perf_counter() - t0
         if i >= warmup:
             times.append(dt)
@@ -147,14 +147,32 @@ def cpu_leg(steps, warmup, nthreads=0, expr_samples=1 << 23, fill_samples=1 << 2
     gbs = (n * 120 + fill_samples * 8) / t / 1e9
     sample = ("expression on %d samples (2^%d) + normal fill of %d doubles (2^%d) per step, median of %d"
               % (n, n.bit_length() - 1, fill_samples, fill_samples.bit_length() - 1, len(times)))
-    return gbs, t, nt, sample
+    return gbs, t, nt, sample, (ins, d_out, z_out)
+
+
+def check_against_oracle(arrs, d, z, ins, d_ref, z_ref):
+    """The GPU step's results on the CPU leg's sample against the oracle's
+    (same seeded inputs): inputs bit for bit, the expression in units of
+    2^-53 of its term scale, the normals in the reference's abs+rel form."""
+    import numpy as np
+    n, nz = d_ref.shape[1], z_ref.shape[1]
+    same_inputs = all(np.array_equal(x.data[:, :n].cpu().numpy(), r[:, :n]) for x, r in zip(arrs, ins))
+    got = d.data[:, :n].cpu().numpy()
+    a, b, c, d0 = (r[:, :n] for r in ins)
+    scale = np.maximum(np.abs(np.sqrt(a * a + b * b) * np.log1p(np.abs(c))), np.abs(1.0 / np.sqrt(1.0 + d0 * d0)))
+    e_expr = float(np.max(np.abs(got - d_ref[:, :n]) / scale)) / 2.0 ** -53
+    gz = z.data[:, :nz].cpu().numpy()
+    e_norm = float(np.max(np.abs(gz - z_ref[:, :nz]) / (1.0 + np.abs(z_ref[:, :nz])))) / 2.0 ** -53
+    return {"inputs_bit_exact": bool(same_inputs), "expr_samples": int(n), "expr_max_err_2m53_of_terms": round(e_expr, 1),
+            "normal_samples": int(nz), "normal_max_err_2m53_abs_rel": round(e_norm, 1),
+            "expr_bound_2m53": 512, "normal_bound_2m53": 256, "reference_normal_tol": 1e-12}
 
 
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    gbs, t, nt, sample = cpu_leg(args.steps, args.warmup)
+    gbs, t, nt, sample, _ = cpu_leg(args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
@@ -639,8 +657,10 @@ def run_ours(args):
                 "fill_frac": round(BYTES_FILL / (tf * 1e-3) / 1e9 / peak, 4)}
     cpu = None
     if not args.no_cpu:
-        gbs, t, nt, sample = cpu_leg(1, 1)
+        gbs, t, nt, sample, ref = cpu_leg(1, 1)
         cpu = {"value": round(gbs, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample}
+        # the oracle doubles as the checker of this run's GPU results
+        cpu["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref)
     secondary = None
     if not args.no_secondary:
         # the other configurations, measured after the timed region

@@ -153,9 +153,12 @@ int main() {
             const ag_u64 seed = 0x1234567ull;
             const ag::q4 x = ag::philox_block(seed, (ag_u32)i, 0u);
             const ag_u64 z = (ag_u64)x.x ^ ((ag_u64)x.y << 21);
-            const LD u = ((LD)z + 0.5L) * 1.1102230246251565404e-16L;
             const ag_u64 zy = (ag_u64)x.z ^ ((ag_u64)x.w << 21);
-            const LD v = ((LD)zy + 0.5L) * 2.2204460492503130808e-16L;
+            // the reference's uniforms are doubles (random/detail/Backend.h):
+            // z 2^-53 + 2^-54 and zy 2^-52 + 2^-53, each rounded once
+            volatile double u0 = (double)z * 1.1102230246251565e-16, v0 = (double)zy * 2.2204460492503131e-16;
+            const LD u = (LD)(double)(u0 + 5.5511151231257827e-17);
+            const LD v = (LD)(double)(v0 + 1.1102230246251565e-16);
             const LD ref = sqrtl(-2.0L * logl(u)) * sinl(v * 3.14159265358979323846264338327950288L);
             const double got = to_double(normal_df(seed, (ag_u32)i, 0u));
             // the unnormalised form reassembles to the same double
