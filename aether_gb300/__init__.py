@@ -157,6 +157,35 @@ class AccumPlane:
         return self
 
 
+class _PinnedChunk:
+    """Owner of one aether_chunk_alloc pinned host chunk (released with it)."""
+
+    def __init__(self, nbytes):
+        self.chunk, self.ptr = ctypes.c_void_p(), ctypes.c_void_p()
+        _abi.check(_abi.lib().aether_chunk_alloc(2, 0, nbytes, None, ctypes.byref(self.chunk), ctypes.byref(self.ptr)))
+
+    def __del__(self):
+        if self.chunk:
+            _abi.lib().aether_chunk_release(self.chunk)
+            self.chunk = ctypes.c_void_p()
+
+
+def pinned_empty(shape, dtype="f64"):
+    """Page-locked host memory from aether_chunk_alloc (kind 2: huge-page
+    backed, registered and device-mapped) as a CPU torch tensor; the chunk is
+    released when the last view of it goes away."""
+    import numpy as np
+    npdt = {"f64": np.float64, "f32": np.float32, "i32": np.int32, "u8": np.uint8}[dtype]
+    n = 1
+    for e in shape:
+        n *= int(e)
+    nbytes = n * np.dtype(npdt).itemsize
+    owner = _PinnedChunk(max(nbytes, 1))
+    buf = (ctypes.c_char * max(nbytes, 1)).from_address(owner.ptr.value)
+    buf._owner = owner   # the array keeps the buffer, the buffer keeps the chunk
+    return _torch().from_numpy(np.frombuffer(buf, dtype=npdt, count=n).reshape(tuple(shape)))
+
+
 def padded_block_samples(n, parts, pad_to=32):
     """Block pitch of a sample-mode partition: ceil(n / parts) rounded up to
     pad_to (residency/Partition.h:61-72)."""
@@ -396,6 +425,7 @@ from .runtime import RuntimeOp, runtime_eval, runtime_view  # noqa: E402
 
 __all__ = [
     "Batch", "RuntimeOp", "runtime_eval", "runtime_view", "padded_block_samples", "partition_view", "AccumPlane",
+    "pinned_empty",
     "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
     "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
     "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",

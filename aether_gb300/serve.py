@@ -107,7 +107,8 @@ class HostPools:
         g = torch.Generator().manual_seed(seed)
         self.pools = {}
         for dt, nbytes, tdt in (("f64", f64_bytes, torch.float64), ("f32", f32_bytes, torch.float32)):
-            t = torch.empty(nbytes // _ES[dt], dtype=tdt, pin_memory=True)
+            from . import pinned_empty
+            t = pinned_empty((nbytes // _ES[dt],), dt)
             t.uniform_(-1.0, 1.0, generator=g)
             self.pools[dt] = t
 

@@ -538,11 +538,12 @@ def run_ours(args):
         L = ag._abi.lib()
         import ctypes
         nb = N_EXPR * 3 * 8
-        host_in = [torch.empty((3, N_EXPR), dtype=torch.float64, pin_memory=True) for _ in range(4)]
+        # host buffers from the C-ABI's pinned chunks (huge-page backed, registered)
+        host_in = [ag.pinned_empty((3, N_EXPR)) for _ in range(4)]
         for h, x in zip(host_in, arrs):
             h.copy_(x.data[:, :N_EXPR])
-        host_out = torch.empty((3, N_EXPR), dtype=torch.float64, pin_memory=True)
-        host_fill = torch.empty((1, N_FILL), dtype=torch.float64, pin_memory=True)
+        host_out = ag.pinned_empty((3, N_EXPR))
+        host_fill = ag.pinned_empty((1, N_FILL))
         # The step cut into K sample blocks (partition_view) through a
         # three-stage pipeline: uploads on one stream, kernels on a second,
         # downloads on a third, joined by events, so block r+1 copies in

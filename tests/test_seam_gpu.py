@@ -35,3 +35,25 @@ def test_seam_table_round_trip():
     L.aether_chunk_release(chunk)
     L.aether_chunk_release(hchunk)
     L.aether_drain()
+
+
+def test_pinned_empty_is_registered_and_round_trips():
+    """Host chunks of kind 2 back ag.pinned_empty: page-locked, device-mapped
+    and released with the last view."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import aether_gb300 as ag
+    from aether_gb300 import _abi
+    L = _abi.lib()
+    h = ag.pinned_empty((3, 1000))
+    h.copy_(torch.arange(3000, dtype=torch.float64).reshape(3, 1000))
+    dev = torch.empty((3, 1000), dtype=torch.float64, device="cuda")
+    P = ctypes.c_void_p
+    _abi.check(L.aether_copy(1, 0, P(dev.data_ptr()), 2, 0, P(h.data_ptr()), 3000 * 8, None))
+    _abi.check(L.aether_stream_sync(0, None))
+    assert torch.equal(dev.cpu(), h)
+    assert torch.cuda.cudart().cudaHostGetFlags is not None
+    # device-mapped: a kernel can read it by address (torch sees host memory)
+    d = ctypes.c_int(-1)
+    assert L.aether_pointer_device(P(h.data_ptr()), ctypes.byref(d)) == 1   # host memory, not a device pointer
+    del h
