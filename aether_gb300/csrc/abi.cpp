@@ -81,17 +81,21 @@ struct Chunk {
 };
 
 // Pinned host memory: anonymous pages with transparent huge pages requested,
-// registered with the driver (mapped, so kernels can read it by address).
-// Measured on GB300 machines: a pipelined upload/compute/download loop over
-// driver-allocated pinned buffers ran at 36-68 ms per step depending on what
-// the box had run before, over these at 36.0 ms every time. Falls back to
-// cudaMallocHost when the mapping or the registration is refused.
+// touched, then registered with the driver (mapped, so kernels can read it by
+// address). Measured on GB300 machines: a pipelined upload/compute/download loop
+// over driver-allocated pinned buffers ran at 36-68 ms per step depending on
+// what the box had run before, over these at 36.0 ms every time. Falls back
+// to cudaMallocHost when the mapping or the registration is refused.
 void pinned_alloc(Chunk& c, size_t b) {
     const size_t huge = size_t(2) << 20;
     const size_t len = (b + huge - 1) / huge * huge;
     void* p = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
     if (p != MAP_FAILED) {
         madvise(p, len, MADV_HUGEPAGE);   // advisory: ignored where huge pages are off
+        // first touch from the CPU, so the pages are faulted in as huge pages
+        // before the driver pins them (pages faulted in by the pinning itself
+        // measured several times slower for DMA)
+        std::memset(p, 0, len);
         if (cudaHostRegister(p, len, cudaHostRegisterMapped | cudaHostRegisterPortable) == cudaSuccess) {
             c.ptr = p;
             c.mapped = len;
