@@ -171,9 +171,9 @@ class _PinnedChunk:
 
 
 def pinned_empty(shape, dtype="f64"):
-    """Page-locked host memory from aether_chunk_alloc (kind 2: huge-page
-    backed, registered and device-mapped) as a CPU torch tensor; the chunk is
-    released when the last view of it goes away."""
+    """Page-locked, device-mapped host memory from aether_chunk_alloc (kind 2)
+    as a CPU torch tensor; the chunk is released when the last view of it
+    goes away."""
     import numpy as np
     npdt = {"f64": np.float64, "f32": np.float32, "i32": np.int32, "u8": np.uint8}[dtype]
     n = 1

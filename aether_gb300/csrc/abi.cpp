@@ -8,7 +8,6 @@
 #include "aether_gb300.h"
 
 #include <cuda_runtime.h>
-#include <sys/mman.h>
 
 #include <algorithm>
 #include <cmath>
@@ -77,35 +76,13 @@ struct Chunk {
     void* ptr = nullptr;
     size_t bytes = 0;
     cudaStream_t stream = nullptr;
-    size_t mapped = 0;   // pinned: bytes of the registered anonymous mapping (0: cudaMallocHost)
 };
 
-// Pinned host memory: anonymous pages with transparent huge pages requested,
-// touched, then registered with the driver (mapped, so kernels can read it by
-// address). Measured on GB300 machines: a pipelined upload/compute/download loop
-// over driver-allocated pinned buffers ran at 36-68 ms per step depending on
-// what the box had run before, over these at 36.0 ms every time. Falls back
-// to cudaMallocHost when the mapping or the registration is refused.
-void pinned_alloc(Chunk& c, size_t b) {
-    const size_t huge = size_t(2) << 20;
-    const size_t len = (b + huge - 1) / huge * huge;
-    void* p = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-    if (p != MAP_FAILED) {
-        madvise(p, len, MADV_HUGEPAGE);   // advisory: ignored where huge pages are off
-        // first touch from the CPU, so the pages are faulted in as huge pages
-        // before the driver pins them (pages faulted in by the pinning itself
-        // measured several times slower for DMA)
-        std::memset(p, 0, len);
-        if (cudaHostRegister(p, len, cudaHostRegisterMapped | cudaHostRegisterPortable) == cudaSuccess) {
-            c.ptr = p;
-            c.mapped = len;
-            return;
-        }
-        cudaGetLastError();
-        munmap(p, len);
-    }
-    ck(cudaMallocHost(&c.ptr, b), "cudaMallocHost");
-}
+// Pinned host memory from the driver (page-locked, device-mapped). Huge-page
+// backed anonymous mappings registered with cudaHostRegister were tried for
+// the bulk host<->device streams and measured inconsistent across boxes:
+// 36.0 ms per pipelined step on one, 4-8 GB/s copies for seconds on others.
+void pinned_alloc(Chunk& c, size_t b) { ck(cudaMallocHost(&c.ptr, b), "cudaMallocHost"); }
 
 std::mutex g_deferred_mu;
 std::vector<Chunk*> g_deferred;
@@ -113,12 +90,7 @@ std::vector<Chunk*> g_deferred;
 void free_now(Chunk* c) {
     if (c->ptr) {
         if (c->kind == AETHER_MEM_CPU) std::free(c->ptr);
-        else if (c->kind == AETHER_MEM_PINNED && c->mapped) {
-            cudaHostUnregister(c->ptr);
-            munmap(c->ptr, c->mapped);
-        } else if (c->kind == AETHER_MEM_PINNED) {
-            cudaFreeHost(c->ptr);
-        }
+        else if (c->kind == AETHER_MEM_PINNED) cudaFreeHost(c->ptr);
         else {
             OnDevice d(c->dev);
             cudaFreeAsync(c->ptr, c->stream);

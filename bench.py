@@ -538,7 +538,7 @@ def run_ours(args):
         L = ag._abi.lib()
         import ctypes
         nb = N_EXPR * 3 * 8
-        # host buffers from the C-ABI's pinned chunks (huge-page backed, registered)
+        # host buffers from the C-ABI's pinned chunks
         host_in = [ag.pinned_empty((3, N_EXPR)) for _ in range(4)]
         for h, x in zip(host_in, arrs):
             h.copy_(x.data[:, :N_EXPR])

@@ -38,8 +38,8 @@ def test_seam_table_round_trip():
 
 
 def test_pinned_empty_is_registered_and_round_trips():
-    """Host chunks of kind 2 back ag.pinned_empty: page-locked, device-mapped
-    and released with the last view."""
+    """Host chunks of kind 2 back ag.pinned_empty: page-locked, copied by the
+    copy engines, and released with the last view."""
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     import aether_gb300 as ag
