@@ -267,9 +267,15 @@ def _as_expr(o, shape):
     return Bcast(s, shape) if shape != () else s
 
 
+# Constants the kernels bake in (a handful of values, so the plan cache stays
+# small): their magnitude bounds let the generator drop range tests.
+_LITERAL_CONSTANTS = (1.0, -1.0, 2.0, 0.5)
+
+
 def constant(value, shape):
     """aether::constant<extents<...>>(v) (expr/nodes/Constant.h:98-150)."""
-    s = Scalar(value)
+    v = float(value)
+    s = Literal(v) if v in _LITERAL_CONSTANTS else Scalar(v)
     return Bcast(s, shape) if tuple(shape) != () else s
 
 

@@ -415,12 +415,23 @@ inline Expr select(const Expr& c, const Expr& a, const Expr& b) {
     return Expr(ir::op("select", {c.node(), a.node(), b.node()}, a.shape()));
 }
 
-/** A runtime scalar broadcast to `Extents` (expr/nodes/Constant.h:98-150). */
+/** A scalar broadcast to `Extents` (expr/nodes/Constant.h:98-150): a runtime
+ *  scalar, except for 1, -1, 2 and 1/2, which the kernels bake in (a handful of
+ *  values, so the plan cache stays small; their magnitude bounds let the
+ *  generator drop range tests). */
+inline ir::NodeP constant_node(double v) {
+    if (v == 1.0 || v == -1.0 || v == 2.0 || v == 0.5) {
+        auto n = std::make_shared<ir::LiteralNode>();
+        n->v = v;
+        return n;
+    }
+    return ir::scalar(v);
+}
 template <class Extents>
 Expr constant(double v) {
-    return Expr(ir::bcast(ir::scalar(v), ir::shape_of(Extents{})));
+    return Expr(ir::bcast(constant_node(v), ir::shape_of(Extents{})));
 }
-inline Expr constant(double v, const ir::Shape& shape) { return Expr(ir::bcast(ir::scalar(v), shape)); }
+inline Expr constant(double v, const ir::Shape& shape) { return Expr(ir::bcast(constant_node(v), shape)); }
 /** A scalar baked into the kernel text (compiled once per value). */
 inline Expr literal(double v) {
     auto n = std::make_shared<ir::LiteralNode>();
