@@ -209,12 +209,16 @@ def test_emulated_uniform_fill_is_bit_exact(oracle):
 
 
 def test_emulated_normal_fill_within_reference_tolerance(oracle):
-    n = 1 << 20
+    # 2^25 draws of the benchmark's fill: among them uniforms within 2^-30 of
+    # 1, where the reference's double u is rounded (sample 18695431), so the
+    # double-float draw must reproduce that rounding to stay inside 1e-12
+    n = 1 << 25
     y = ag.Array("f64", (1,), n)
     ag.assign(y, ag.Generator(7).substream(4).normal(1, 0.0, 1.0), math=1)
     r = oracle.fill_normal_f64(ag.Generator(7).substream(4).key, 0.0, 1.0, 1, n)
     err = np.abs(y.host() - r) / (1 + np.abs(r))
-    assert err.max() <= 1e-12, err.max()
+    assert err.max() <= 256 * 2.0 ** -53, err.max() / 2.0 ** -53
+    assert err[0, 18695431] <= 256 * 2.0 ** -53
 
 
 def test_emulated_fallback_reproduces_native_on_special_inputs():
