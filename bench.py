@@ -705,7 +705,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default lowering instead of the autotuned one")
     ap.add_argument("--no-secondary", action="store_true", help="skip configs 1, 3, 4 and 5 after the timed region")
-    ap.add_argument("--e2e-chunks", type=int, default=16, help="sample blocks of the pipelined end-to-end step")
+    ap.add_argument("--e2e-chunks", type=int, default=4, help="sample blocks of the pipelined end-to-end step")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
     args = ap.parse_args()
