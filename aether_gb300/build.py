@@ -24,7 +24,8 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp", "serve.cpp", "tables.cpp"]
 DEVICE_SOURCES = ["noalloc.cu", "runtime.cu", "serve_copy.cu"]
 EMBED = [("kAgDeviceSrc", "device/ag_device.cuh"), ("kAgEmu64Src", "device/ag_emu64.cuh"),
-         ("kAgEmu64TablesSrc", "device/ag_emu64_tables.cuh")]
+         ("kAgEmu64TablesSrc", "device/ag_emu64_tables.cuh"), ("kAgEmu64BmSrc", "device/ag_emu64_bm.cuh"),
+         ("kAgEmu64BmTablesSrc", "device/ag_emu64_bm_tables.cuh")]
 EXPORT_PREFIX = "aether_"
 
 

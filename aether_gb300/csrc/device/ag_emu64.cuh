@@ -278,17 +278,6 @@ __device__ __forceinline__ df from_u64(ag_u64 w) {
     return fast_two_sum(h, l);
 }
 __device__ __forceinline__ float p2f(int k) { return __int_as_float((k + 127) << 23); }   // 2^k, |k| <= 126
-// sgn w 2^-54 for 0 < w < 2^54: normalised so the leading bit sits at 2^53,
-// the top 24 bits exact and the next 30 rounded once (2^-48 relative); the
-// pair is left with |lo| < ulp(hi). sgn is the sign bit (0 or 0x80000000).
-__device__ __forceinline__ df from_u54_2m54(ag_u64 w, ag_u32 sgn) {
-    const int lz = __clzll((long long)w) - 10;   // 0 .. 53
-    const ag_u64 wn = w << lz;                    // [2^53, 2^54)
-    const ag_u32 sc = ((ag_u32)(103 - lz) << 23) | sgn;   // +-2^(-24-lz): 2^30 units of wn, times 2^-54
-    const float h = __fmul_rn(__uint2float_rn((ag_u32)(wn >> 30)), __int_as_float(sc));
-    const float l = __fmul_rn(__uint2float_rn((ag_u32)wn & 0x3fffffffu), __int_as_float(sc - (30u << 23)));
-    return mk(h, l);
-}
 // Round to nearest integer for |x| < 2^22 with one FP32 add (no conversion unit).
 __device__ __forceinline__ float rint_f(float x) { return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f); }
 __device__ __forceinline__ int rint_i(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000; }
@@ -602,49 +591,12 @@ __device__ __forceinline__ df sinpi_(df v) {
 // ---------------------------------------------------------------------------
 // Philox draws as double-floats. Uniform: (2w+1) 2^-33 is exact in a
 // double-float, so uniform(lo, hi) fills with power-of-two ranges are
-// bit-exact. Normal: Box-Muller from the exact 54-bit integers of u and v
-// (random/detail/Backend.h:209-236); log(u) is taken as log(u) for u < 1/2 and
-// as log1p(-(1-u)) above, with 1-u formed in integer arithmetic.
+// bit-exact. The normal draw (Box-Muller) is in ag_emu64_bm.cuh, which plans
+// with normal leaves include.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ df draw01_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag_u32 w = ag::philox_block(seed, g, c).x;
     return scale(from_u64(2ull * w + 1ull), p2f(-33));
-}
-// U: the product is left unnormalised (the draw is only reassembled into a double)
-template <bool U = false>
-__device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
-    const ag::q4 x = ag::philox_block(seed, g, c);
-    // u is the reference's double z 2^-53 + 2^-54 (random/detail/Backend.h
-    // uniformDoubleHq): exact below 1/2, rounded to even above it, where it is
-    // k 2^-53 with k = z + (z & 1). So u = w 2^-54 with w = 2 z + 1 below 1/2,
-    // and 1 - u = w 2^-54 with w = 2^54 - 2 k (even, at most 2^53) above it.
-    const ag_u64 z = (ag_u64)x.x ^ ((ag_u64)x.y << 21);
-    const bool lower = z < (1ull << 52);
-    const ag_u64 w = lower ? 2ull * z + 1ull : (1ull << 54) - 2ull * (z + (z & 1ull));
-    // log(u) for u in [2^-54, 1/2) or log1p(-w) for w in [0, 1/2]; w = 0 (u
-    // rounded to 1) gives a zero argument to the square root below, whose NaN
-    // sends the lane to the native path
-    const df L = log_s<false, LOG_SRT>(lower ? 0.0f : 1.0f, from_u54_2m54(w, lower ? 0u : 0x80000000u));
-    const df sv = sqrt_pos_(scale(L, -2.0f));   // log u < 0: the argument is positive
-    // v is the reference's double zy 2^-52 + 2^-53: exact below 1, rounded to
-    // even above it. So v = V 2^-53 with V = 2 zy + 1, or 2 (zy + (zy & 1))
-    // for zy >= 2^52, V <= 2^54. In integers: K = round(V / 2^41) counts steps
-    // of 1/4096 half-turn, q = round(K / 2048) is the quadrant, j = K - 2048 q
-    // in [-1024, 1024] the table point pi j/4096, and R = V - 2^41 K (|R| <=
-    // 2^40) the remainder, exact in a double-float: sin(pi v) keeps full
-    // relative accuracy next to the zeros of the sine.
-    const ag_u64 zy = (ag_u64)x.z ^ ((ag_u64)x.w << 21);
-    const ag_u64 V = zy < (1ull << 52) ? 2ull * zy + 1ull : 2ull * (zy + (zy & 1ull));
-    const ag_u32 vh = (ag_u32)(V >> 32), vl = (ag_u32)V;
-    const ag_u32 K = (vh + 256u) >> 9;   // (V + 2^40) >> 41
-    const int q = (int)((K + 1024u) >> 11);
-    const int j = (int)K - (q << 11);
-    const ag_u32 rh = vh - (K << 9);   // R = rh 2^32 + vl, rh in [-256, 255] as a signed word
-    // R = Rh 2^17 + Rl with Rh = floor(R / 2^17) (|Rh| <= 2^23) and 0 <= Rl < 2^17
-    const int Rh = (int)((rh << 15) | (vl >> 17));
-    const df t = fast_two_sum(__fmul_rn((float)Rh, p2f(-36)), __fmul_rn((float)(vl & 0x1ffffu), p2f(-53)));
-    const df sn = trig_tail(ld4(kSinCosPi4096, j + AG_SCPI_TAB_OFF), mul(t, mk(AG_PI_HI, AG_PI_LO)), q, false);
-    return U ? mul_u(sv, sn) : mul(sv, sn);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,5 +1,6 @@
-"""Generate ag_emu64_tables.cuh: the tables and split constants of the
-double-float (float hi + float lo) function kernels in ag_emu64.cuh.
+"""Generate ag_emu64_tables.cuh and ag_emu64_bm_tables.cuh: the tables and
+split constants of the double-float (float hi + float lo) function kernels in
+ag_emu64.cuh and of the Box-Muller draw in ag_emu64_bm.cuh.
 
 Every value is computed here with mpmath at 200 bits and rounded twice to
 float (hi = fl(v), lo = fl(v - hi)), so hi + lo carries about 48 bits.
@@ -111,15 +112,6 @@ def main():
         out.append("#define AG_2OPI_W%d 0x%016xull" % (k, w))
     out.append("#define AG_SC_TAB_OFF 1664")
     out.append("__device__ __align__(16) const float kSinCos2048[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
-    # sin/cos(pi j/4096), j in [-1024, 1024], packed like the table above: the
-    # Box-Muller angle pi v is reduced in integers to a quadrant, one of these
-    # points and an exact remainder of at most pi 2^-13.
-    packed = []
-    for j in range(-1024, 1025):
-        a = mp.pi * mp.mpf(j) / 4096
-        packed += list(split2(mp.sin(a))) + list(split2(mp.cos(a)))
-    out.append("#define AG_SCPI_TAB_OFF 1024")
-    out.append("__device__ __align__(16) const float kSinCosPi4096[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)))
     # pi/2 in three parts: the first with 12 bits so k*P1 is exact for |k| < 2^12.
     pio2 = mp.pi / 2
     p1 = trunc_bits(pio2, 12)
@@ -138,6 +130,20 @@ def main():
     out += ["}  // namespace e64", "}  // namespace ag", ""]
     with open(os.path.join(HERE, "ag_emu64_tables.cuh"), "w") as f:
         f.write("\n".join(out))
+
+    # The Box-Muller sine: sin/cos(pi k/4096) over the whole period, k in
+    # [0, 8192], packed (S hi, S lo, C hi, C lo). The angle pi v is reduced in
+    # integers to one of these points and an exact remainder of at most
+    # pi 2^-13, with no quadrant step. Included only by plans that draw normals.
+    packed = []
+    for k in range(0, 8193):
+        a = mp.pi * mp.mpf(k) / 4096
+        packed += list(split2(mp.sin(a))) + list(split2(mp.cos(a)))
+    bm = ["// generated by gen_emu64_tables.py -- do not edit", "#pragma once", "namespace ag {", "namespace e64 {",
+          "__device__ __align__(16) const float kSinCosPiPeriod[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)),
+          "}  // namespace e64", "}  // namespace ag", ""]
+    with open(os.path.join(HERE, "ag_emu64_bm_tables.cuh"), "w") as f:
+        f.write("\n".join(bm))
 
 
 if __name__ == "__main__":

@@ -78,12 +78,14 @@ std::unordered_map<uint64_t, std::string> g_mem;
 
 }  // namespace
 
-int payload_count() { return 3; }
+int payload_count() { return 5; }
 
 bool payload_header(int i, const char** name, const char** src) {
-    static const char* const names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh"};
-    static const char* const srcs[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc};
-    if (i < 0 || i >= 3) return false;
+    static const char* const names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh", "ag_emu64_bm.cuh",
+                                        "ag_emu64_bm_tables.cuh"};
+    static const char* const srcs[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc, kAgEmu64BmSrc,
+                                       kAgEmu64BmTablesSrc};
+    if (i < 0 || i >= 5) return false;
     *name = names[i];
     *src = srcs[i];
     return true;
@@ -101,10 +103,11 @@ uint64_t payload_digest() {
 }
 
 std::string compile_for_arch(const std::string& source, const std::string& arch) {
-    const char* hdr_src[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc};
-    const char* hdr_names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh"};
+    const char* hdr_src[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc, kAgEmu64BmSrc, kAgEmu64BmTablesSrc};
+    const char* hdr_names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh", "ag_emu64_bm.cuh",
+                               "ag_emu64_bm_tables.cuh"};
     nvrtcProgram prog;
-    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_plan.cu", 3, hdr_src, hdr_names) != NVRTC_SUCCESS)
+    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_plan.cu", 5, hdr_src, hdr_names) != NVRTC_SUCCESS)
         throw std::runtime_error("nvrtcCreateProgram failed");
     const std::string arch_opt = "--gpu-architecture=" + arch;
     const char* opts[] = {arch_opt.c_str(), "--std=c++17", "--fmad=true", "--dopt=on"};

@@ -941,6 +941,14 @@ std::string kernel_base(const Plan& plan, const std::string& text) {
     return buf;
 }
 
+// Plans with normal or lognormal leaves include the Box-Muller header when
+// lowered to double-float.
+bool draws_normals(const Plan& P) {
+    for (const Node& n : P.nodes)
+        if (n.op == "normal" || n.op == "lognormal") return true;
+    return false;
+}
+
 std::string generate_source(const Plan& plan_in, const Lowering& low, const std::string& base,
                             const std::string& suffix, bool chunk_only) {
     // Re-derive the sample contexts (at0 subtrees) from the node graph: every
@@ -985,6 +993,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         o << "// generated by aether_gb300 from an aether-ir/1 plan\n";
         o << "#include \"ag_device.cuh\"\n";
         if (low.math >= 1) o << "#include \"ag_emu64.cuh\"\n";
+        if (low.math >= 1 && draws_normals(P)) o << "#include \"ag_emu64_bm.cuh\"\n";
         o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
     }
     const std::string W = g.W, S = g.S;
@@ -1210,6 +1219,9 @@ std::string generate_batch_source(const std::vector<const Plan*>& plans, const s
     o << "// generated by aether_gb300: batch of " << plans.size() << " plans\n";
     o << "#include \"ag_device.cuh\"\n";
     if (emu) o << "#include \"ag_emu64.cuh\"\n";
+    bool bm = false;
+    for (size_t p = 0; p < plans.size(); ++p) bm = bm || (lows[p].math >= 1 && draws_normals(*plans[p]));
+    if (bm) o << "#include \"ag_emu64_bm.cuh\"\n";
     o << "#define AG_BLOCK " << block << "\n#define AG_IPT " << ipt << "\n";
     std::vector<int> vecs;
     for (size_t p = 0; p < plans.size(); ++p) {

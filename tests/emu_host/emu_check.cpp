@@ -4,6 +4,7 @@
 #include "host_shim.h"
 
 #include "../../aether_gb300/csrc/device/ag_emu64.cuh"
+#include "../../aether_gb300/csrc/device/ag_emu64_bm.cuh"
 
 #include <cstdio>
 #include <random>

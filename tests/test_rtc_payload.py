@@ -29,7 +29,8 @@ extern "C" __global__ void user_kernel(double* out, unsigned long long key, unsi
 
 def test_payload_headers_and_digest():
     p = rtc.payload()
-    assert set(p.headers) == {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh"}
+    assert set(p.headers) == {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh", "ag_emu64_bm.cuh",
+                              "ag_emu64_bm_tables.cuh"}
     assert all(len(v) > 1000 for v in p.headers.values())
     assert len(p.digest) == 16 and rtc.payload().digest == p.digest
 
