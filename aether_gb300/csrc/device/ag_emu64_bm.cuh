@@ -6,8 +6,8 @@
 // only) from the reference's own double uniforms u and v, reproduced exactly
 // in integers; log(u) is taken as log(u) for u < 1/2 and as log1p(-(1-u))
 // above, with 1-u formed in integers; sin(pi v) is reduced in integers to a
-// point of a table of sin/cos(pi k/4096) over the whole period and an exact
-// remainder.
+// point of a table of sin and pi cos of pi k/4096 over the whole period and an
+// exact remainder.
 #pragma once
 
 #include "ag_emu64_bm_tables.cuh"
@@ -27,17 +27,22 @@ __device__ __forceinline__ df from_u54_2m54(ag_u64 w, ag_u32 sgn) {
     return mk(h, l);
 }
 
-// sin(pi k/4096 + r) from the table entry (S, C) of k and |r| <= pi 2^-13:
-// S (1 + cm1) + C st with st = sin r = r + r^3 (-1/6 + r^2/120) and cm1 =
-// cos r - 1 = r^2 (-1/2 + r^2/24); the cubic and quadratic terms are float.
+// sin(pi (k/4096 + t)) from the table entry (S, pi C) of k and the exact
+// remainder |t| <= 2^-13 in half-turns: with r = pi t, S (1 + cm1) + C st,
+// st = sin r = r + r^3 (-1/6 + r^2/120) and cm1 = cos r - 1 = r^2 (-1/2 +
+// r^2/24). C r = (pi C) t and C r^3 = (pi C) t r^2, so only the float r of the
+// small terms needs pi; the leading product is (pi C) t in double-float.
 // |S| >= sin(pi/4096) >= |C r| except where S = 0: the sum is led by S.
-__device__ __forceinline__ df sin_from_period_table(const f4& sc, df r) {
-    const float th = r.hi;
-    const float th2 = __fmul_rn(th, th);
-    const float cubic = __fmul_rn(__fmul_rn(th, th2), __fmaf_rn(th2, 8.33333333e-3f, -1.66666667e-1f));
-    const float cm1 = __fmul_rn(th2, __fmaf_rn(th2, 4.16666667e-2f, -0.5f));
-    const df S = mk(sc.x, sc.y), C = mk(sc.z, sc.w);
-    return add_quick(add_quick(S, mul_u(C, r)), __fmaf_rn(S.hi, cm1, __fmul_rn(C.hi, cubic)));
+__device__ __forceinline__ df sin_from_period_table(const f4& sc, df t) {
+    const float th = t.hi;
+    // r = pi t rounded once (pi's and t's low parts joined by FMA): the
+    // quadratic term needs r to float accuracy
+    const float rh = __fmaf_rn(AG_PI_HI, th, __fmaf_rn(AG_PI_HI, t.lo, __fmul_rn(AG_PI_LO, th)));
+    const float rh2 = __fmul_rn(rh, rh);
+    const float cub = __fmul_rn(__fmul_rn(th, rh2), __fmaf_rn(rh2, 8.33333333e-3f, -1.66666667e-1f));
+    const float cm1 = __fmul_rn(rh2, __fmaf_rn(rh2, 4.16666667e-2f, -0.5f));
+    const df S = mk(sc.x, sc.y), PC = mk(sc.z, sc.w);
+    return add_quick(add_quick(S, mul_u(PC, t)), __fmaf_rn(S.hi, cm1, __fmul_rn(PC.hi, cub)));
 }
 
 // U: the product is left unnormalised (the draw is only reassembled into a double)
@@ -70,7 +75,7 @@ __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     // R = Rh 2^17 + Rl with Rh = floor(R / 2^17) (|Rh| <= 2^23) and 0 <= Rl < 2^17
     const int Rh = (int)((rh << 15) | (vl >> 17));
     const df t = fast_two_sum(__fmul_rn((float)Rh, p2f(-36)), __fmul_rn((float)(vl & 0x1ffffu), p2f(-53)));
-    const df sn = sin_from_period_table(ld4(kSinCosPiPeriod, (int)K), mul(t, mk(AG_PI_HI, AG_PI_LO)));
+    const df sn = sin_from_period_table(ld4(kSinCosPiPeriod, (int)K), t);
     return U ? mul_u(sv, sn) : mul(sv, sn);
 }
 

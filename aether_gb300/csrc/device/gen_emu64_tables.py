@@ -131,14 +131,16 @@ def main():
     with open(os.path.join(HERE, "ag_emu64_tables.cuh"), "w") as f:
         f.write("\n".join(out))
 
-    # The Box-Muller sine: sin/cos(pi k/4096) over the whole period, k in
-    # [0, 8192], packed (S hi, S lo, C hi, C lo). The angle pi v is reduced in
-    # integers to one of these points and an exact remainder of at most
-    # pi 2^-13, with no quadrant step. Included only by plans that draw normals.
+    # The Box-Muller sine: sin(pi k/4096) and pi cos(pi k/4096) over the whole
+    # period, k in [0, 8192], packed (S hi, S lo, pi C hi, pi C lo). The angle
+    # pi v is reduced in integers to one of these points and an exact remainder
+    # t of at most 2^-13 half-turns, with no quadrant step; the factor pi of
+    # the remainder's leading term rides on the table (C pi t = (pi C) t).
+    # Included only by plans that draw normals.
     packed = []
     for k in range(0, 8193):
         a = mp.pi * mp.mpf(k) / 4096
-        packed += list(split2(mp.sin(a))) + list(split2(mp.cos(a)))
+        packed += list(split2(mp.sin(a))) + list(split2(mp.pi * mp.cos(a)))
     bm = ["// generated by gen_emu64_tables.py -- do not edit", "#pragma once", "namespace ag {", "namespace e64 {",
           "__device__ __align__(16) const float kSinCosPiPeriod[%d] = {%s};" % (len(packed), ", ".join(fl(v) for v in packed)),
           "}  // namespace e64", "}  // namespace ag", ""]
