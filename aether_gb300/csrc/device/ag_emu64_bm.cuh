@@ -12,18 +12,36 @@
 
 #include "ag_emu64_bm_tables.cuh"
 
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+#define AG_NOINLINE __noinline__
+#else
+#define AG_NOINLINE __attribute__((noinline))
+#endif
+
 namespace ag {
 namespace e64 {
 
 // sgn w 2^-54 for 0 < w < 2^54: normalised so the leading bit sits at 2^53,
 // the top 24 bits exact and the next 30 rounded once (2^-48 relative); the
 // pair is left with |lo| < ulp(hi). sgn is the sign bit (0 or 0x80000000).
-__device__ __forceinline__ df from_u54_2m54(ag_u64 w, ag_u32 sgn) {
+__device__ AG_NOINLINE df from_u54_2m54_any(ag_u64 w, ag_u32 sgn) {
     const int lz = __clzll((long long)w) - 10;   // 0 .. 53
     const ag_u64 wn = w << lz;                    // [2^53, 2^54)
     const ag_u32 sc = ((ag_u32)(103 - lz) << 23) | sgn;   // +-2^(-24-lz): 2^30 units of wn, times 2^-54
     const float h = __fmul_rn(__uint2float_rn((ag_u32)(wn >> 30)), __int_as_float(sc));
     const float l = __fmul_rn(__uint2float_rn((ag_u32)wn & 0x3fffffffu), __int_as_float(sc - (30u << 23)));
+    return mk(h, l);
+}
+// The same in 32-bit words when w >= 2^32 (all but 2^-22 of the draws: the
+// normalising shift stays below 32), the general form out of line otherwise.
+__device__ __forceinline__ df from_u54_2m54(ag_u64 w, ag_u32 sgn) {
+    const ag_u32 hi = (ag_u32)(w >> 32), lo = (ag_u32)w;
+    if (hi == 0u) return from_u54_2m54_any(w, sgn);
+    const int lz = __clz((int)hi) - 10;   // 0 .. 21
+    const ag_u32 nh = __funnelshift_l(lo, hi, (unsigned)lz), nl = lo << lz;   // w << lz in [2^53, 2^54)
+    const ag_u32 sc = ((ag_u32)(103 - lz) << 23) | sgn;
+    const float h = __fmul_rn(__uint2float_rn(__funnelshift_l(nl, nh, 2u)), __int_as_float(sc));   // top 24 bits
+    const float l = __fmul_rn(__uint2float_rn(nl & 0x3fffffffu), __int_as_float(sc - (30u << 23)));
     return mk(h, l);
 }
 

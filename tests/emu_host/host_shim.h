@@ -85,4 +85,5 @@ inline double f_pow(double a, double b) { return std::pow(a, b); }
 inline double f_atan2(double a, double b) { return std::atan2(a, b); }
 inline double f_hypot(double a, double b) { return std::hypot(a, b); }
 }  // namespace ag
+inline int __clz(int x) { return x == 0 ? 32 : __builtin_clz((unsigned)x); }
 inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll((unsigned long long)x); }
