@@ -138,6 +138,9 @@ def test_emulated_products_are_range_checked_only_where_bounds_need_it():
     src = _fast_path(_abi.generate(plan_text("f64", (3,), "set", cfg2a, IrContext()), _abi.lowering(math=1)))
     assert "ag::e64::ck(" not in src
     assert src.count("ag::e64::from_double_ck(") == 12
+    # constant(1.0) is baked in, so the bounds also keep the output in range
+    assert "(lit 0x1.0000000000000p+0)" in plan_text("f64", (3,), "set", cfg2a, IrContext())
+    assert "out_ok(" not in src
     src = _fast_path(_abi.generate(plan_text("f64", (3,), "set", (a * b) * c, IrContext()), _abi.lowering(math=1)))
     assert src.count("ag::e64::ck(") == 3          # the outer product, once per component
     src = _fast_path(_abi.generate(plan_text("f64", (3,), "set", ag.cwiseExp(a) * b, IrContext()),
