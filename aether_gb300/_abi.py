@@ -144,6 +144,8 @@ _SIGS = {
     "aether_rtc_header": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                          ctypes.POINTER(ctypes.c_char_p)]),
     "aether_rtc_digest": (ctypes.c_uint64, []),
+    "aether_plan_cache_key": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                             ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64)]),
 }
 
 _lib = None

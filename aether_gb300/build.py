@@ -19,6 +19,10 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libaether_gb300.so")
+# The same objects linked as the reference's CUDA plugin: exactly one exported
+# symbol, aether_memory_v1 (dsc/src/plugin.map:1-4), under the file name the
+# reference's loader opens next to its module (dsc/src/aether_core.cpp:98-101).
+PLUGIN = os.path.join(LIBDIR, "libaether_cuda.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp", "serve.cpp", "tables.cpp"]
@@ -62,6 +66,7 @@ def _embed():
 def _exports():
     text = "{\n  global: %s*;\n  local: *;\n};\n" % EXPORT_PREFIX
     _write_if_changed(os.path.join(BUILD, "exports.map"), text)
+    _write_if_changed(os.path.join(BUILD, "plugin.map"), "{\n  global: aether_memory_v1;\n  local: *;\n};\n")
 
 
 def _stale(obj, deps):
@@ -112,17 +117,20 @@ def build(force=False, verbose=False):
                 sys.stderr.write(" ".join(j) + "\n" + r.stdout + r.stderr)
             if r.returncode:
                 raise RuntimeError("compile failed: " + j[-len(inc) - 1 if False else 0] + " " + " ".join(j[:6]))
-    if force or jobs or not os.path.exists(LIB):
+    if force or jobs or not os.path.exists(LIB) or not os.path.exists(PLUGIN):
         libdir = os.path.join(cuda, "lib64")
         if not os.path.isdir(libdir):
             libdir = os.path.join(cuda, "lib")
-        cmd = ["g++", "-shared", "-o", LIB] + objs + [
-            "-L" + libdir, "-lcudart_static", "-lnvrtc", "-ldl", "-lpthread", "-lrt",
-            "-Wl,-rpath," + libdir, "-Wl,--version-script=" + os.path.join(BUILD, "exports.map"),
-            "-Wl,--no-undefined"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode:
-            raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        links = []
+        for out, vmap in ((LIB, "exports.map"), (PLUGIN, "plugin.map")):
+            links.append(["g++", "-shared", "-o", out] + objs + [
+                "-L" + libdir, "-lcudart_static", "-lnvrtc", "-ldl", "-lpthread", "-lrt",
+                "-Wl,-rpath," + libdir, "-Wl,--version-script=" + os.path.join(BUILD, vmap),
+                "-Wl,--no-undefined"])
+        with cf.ThreadPoolExecutor(max_workers=2) as ex:
+            for cmd, r in zip(links, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), links)):
+                if r.returncode:
+                    raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     return LIB
 
 

@@ -8,6 +8,7 @@
 #include "aether_gb300.h"
 
 #include <cuda_runtime.h>
+#include <nvrtc.h>
 
 #include <algorithm>
 #include <cmath>
@@ -446,6 +447,58 @@ bool make_args(const PlanObj* P, const AetherLaunch* a, AgArgsHost& k) {
     return aligned;
 }
 
+namespace {
+
+void launch_plan_kernel(const PlanObj& P, AgArgsHost& k, uint64_t n, bool vect, cudaStream_t s) {
+    const uint64_t per = chunk_samples(P, vect);
+    const uint64_t nch = (n + per - 1) / per;
+    const int bps = vect ? P.blocks_per_sm_v : P.blocks_per_sm_s;
+    const uint64_t cap = uint64_t(std::max(bps, 1)) * uint64_t(P.sms);
+    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min(nch, cap)));
+    void* params[] = {&k};
+    ck(cudaLaunchKernel(reinterpret_cast<const void*>(vect ? P.fv : P.fs), dim3(grid), dim3(unsigned(P.low.block)),
+                        params, 0, s),
+       "cudaLaunchKernel");
+}
+
+// A default workspace of at least `need` bytes that no launch still running
+// on another stream uses (caller holds P.ws_mu). Preference: an entry last
+// used on `s` itself, then an idle entry that is large enough, then an idle
+// entry grown to `need`, then a new entry. The per-thread default stream is
+// one handle for many streams, so it only reuses idle entries.
+PlanObj::Workspace& acquire_workspace(PlanObj& P, uint64_t need, cudaStream_t s) {
+    auto idle = [](PlanObj::Workspace& w) {
+        const cudaError_t e = cudaEventQuery(w.done);
+        if (e == cudaErrorNotReady) {
+            cudaGetLastError();
+            return false;
+        }
+        ck(e, "cudaEventQuery(workspace)");
+        return true;
+    };
+    for (PlanObj::Workspace& w : P.ws)
+        if (w.ordered && w.last_stream == s && s != cudaStreamPerThread && w.bytes >= need) return w;
+    PlanObj::Workspace* grow = nullptr;
+    for (PlanObj::Workspace& w : P.ws) {
+        if (!idle(w)) continue;
+        if (w.bytes >= need) return w;
+        if (!grow) grow = &w;
+    }
+    if (!grow) {
+        P.ws.emplace_back();
+        grow = &P.ws.back();
+        ck(cudaEventCreateWithFlags(&grow->done, cudaEventDisableTiming), "cudaEventCreate(workspace)");
+    }
+    if (grow->ptr) ck(cudaFree(grow->ptr), "cudaFree(workspace)");
+    grow->ptr = nullptr;
+    grow->bytes = 0;
+    ck(cudaMalloc(&grow->ptr, need), "cudaMalloc(workspace)");
+    grow->bytes = need;
+    return *grow;
+}
+
+}  // namespace
+
 AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream) {
     return guarded([&] {
         PlanObj* P = static_cast<PlanObj*>(plan);
@@ -467,28 +520,26 @@ AG_EXPORT int aether_plan_launch(void* plan, const AetherLaunch* a, void* stream
                 k.ws = static_cast<char*>(a->workspace);
                 k.ws_bytes = a->workspace_bytes;
             } else {
-                std::lock_guard<std::mutex> lk(P->ws_mu);
-                if (P->ws_bytes < need) {
-                    if (P->ws) ck(cudaFree(P->ws), "cudaFree");
-                    P->ws = nullptr;
-                    P->ws_bytes = 0;
-                    ck(cudaMalloc(&P->ws, need), "cudaMalloc(workspace)");
-                    P->ws_bytes = need;
-                }
-                k.ws = static_cast<char*>(P->ws);
-                k.ws_bytes = P->ws_bytes;
+                if (capturing(s))
+                    throw std::runtime_error(
+                        "plan_launch: a sum plan recorded into a CUDA graph needs its own workspace "
+                        "(args->workspace, aether_plan_workspace_size bytes) or aether_plan_launch_noalloc");
+                std::unique_lock<std::mutex> lk(P->ws_mu);
+                PlanObj::Workspace& w = acquire_workspace(*P, need, s);
+                k.ws = static_cast<char*>(w.ptr);
+                k.ws_bytes = w.bytes;
+                ck(cudaMemsetAsync(k.ws, 0, 16, s), "cudaMemsetAsync(counter)");
+                launch_plan_kernel(*P, k, a->n, vect, s);
+                // the entry is busy until this event completes, except for
+                // later launches on the same stream, which run after it
+                ck(cudaEventRecord(w.done, s), "cudaEventRecord(workspace)");
+                w.last_stream = s;
+                w.ordered = s != cudaStreamPerThread;
+                return;
             }
             ck(cudaMemsetAsync(k.ws, 0, 16, s), "cudaMemsetAsync(counter)");
         }
-        const uint64_t per = chunk_samples(*P, vect);
-        const uint64_t nch = (a->n + per - 1) / per;
-        const int bps = vect ? P->blocks_per_sm_v : P->blocks_per_sm_s;
-        const uint64_t cap = uint64_t(std::max(bps, 1)) * uint64_t(P->sms);
-        const unsigned grid = unsigned(std::max<uint64_t>(1, std::min(nch, cap)));
-        void* params[] = {&k};
-        ck(cudaLaunchKernel(reinterpret_cast<const void*>(vect ? P->fv : P->fs), dim3(grid), dim3(unsigned(P->low.block)),
-                            params, 0, s),
-           "cudaLaunchKernel");
+        launch_plan_kernel(*P, k, a->n, vect, s);
     });
 }
 
@@ -725,10 +776,27 @@ AG_EXPORT int aether_nvrtc_check(const char* source, const char* arch) {
     });
 }
 
+AG_EXPORT int aether_plan_cache_key(const char* source, const char* arch, const char* tag, int header_index,
+                                    const char* header_source, uint64_t* key) {
+    return guarded([&] {
+        if (!source || !arch || !tag || !key) throw std::runtime_error("plan_cache_key: null argument");
+        if (header_index >= ag::payload_count())
+            throw std::runtime_error("plan_cache_key: header index " + std::to_string(header_index) + " of " +
+                                     std::to_string(ag::payload_count()));
+        int major = 0, minor = 0;
+        nvrtcVersion(&major, &minor);
+        *key = ag::cache_key(source, arch, tag, major, minor, header_index, header_source);
+    });
+}
+
 AG_EXPORT void aether_plan_release(void* plan) {
     PlanObj* P = static_cast<PlanObj*>(plan);
     if (!P) return;
-    if (P->ws) cudaFree(P->ws);
+    for (PlanObj::Workspace& w : P->ws) {
+        if (w.done) cudaEventSynchronize(w.done);
+        if (w.ptr) cudaFree(w.ptr);
+        if (w.done) cudaEventDestroy(w.done);
+    }
     if (P->library) cudaLibraryUnload(P->library);
     delete P;
 }

@@ -49,10 +49,19 @@ struct PlanObj {
     int blocks_per_sm_v = 1, blocks_per_sm_s = 1;
     int sms = 1;
     int dev = 0;
-    // default workspace of sum plans
+    // Default workspaces of sum plans (launches with args->workspace == NULL):
+    // a pool, so launches on different streams never share scratch. An entry
+    // is reused by a later launch on the same stream (stream order) or once
+    // the event recorded after its last launch has completed.
+    struct Workspace {
+        void* ptr = nullptr;
+        size_t bytes = 0;
+        cudaStream_t last_stream = nullptr;
+        bool ordered = false;          // last_stream orders later launches on it
+        cudaEvent_t done = nullptr;    // recorded after the last launch
+    };
     std::mutex ws_mu;
-    void* ws = nullptr;
-    size_t ws_bytes = 0;
+    std::vector<Workspace> ws;
 };
 
 // One work-list entry of a batched kernel (the AgItem of the generated source).

@@ -22,7 +22,7 @@
 #include <unistd.h>
 #include <unordered_map>
 
-#include "embedded.inc"   // kAgDeviceSrc, kAgEmu64Src
+#include "embedded.inc"   // kAgDeviceSrc, kAgEmu64Src, ... (the device headers as literals)
 
 namespace ag {
 
@@ -78,36 +78,64 @@ std::unordered_map<uint64_t, std::string> g_mem;
 
 }  // namespace
 
-int payload_count() { return 5; }
+namespace {
+
+// The device headers every generated kernel may include, by include name.
+// One table serves the NVRTC program, the payload export and the cache key,
+// so a header added here is covered by all three.
+struct Header {
+    const char* name;
+    const char* src;
+};
+const Header kHeaders[] = {
+    {"ag_device.cuh", kAgDeviceSrc},           {"ag_emu64.cuh", kAgEmu64Src},
+    {"ag_emu64_tables.cuh", kAgEmu64TablesSrc}, {"ag_emu64_bm.cuh", kAgEmu64BmSrc},
+    {"ag_emu64_bm_tables.cuh", kAgEmu64BmTablesSrc},
+};
+constexpr int kNumHeaders = int(sizeof(kHeaders) / sizeof(kHeaders[0]));
+
+}  // namespace
+
+int payload_count() { return kNumHeaders; }
 
 bool payload_header(int i, const char** name, const char** src) {
-    static const char* const names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh", "ag_emu64_bm.cuh",
-                                        "ag_emu64_bm_tables.cuh"};
-    static const char* const srcs[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc, kAgEmu64BmSrc,
-                                       kAgEmu64BmTablesSrc};
-    if (i < 0 || i >= 5) return false;
-    *name = names[i];
-    *src = srcs[i];
+    if (i < 0 || i >= kNumHeaders) return false;
+    *name = kHeaders[i].name;
+    *src = kHeaders[i].src;
     return true;
 }
 
 uint64_t payload_digest() {
     uint64_t h = fnv1a(std::string("aether_gb300 rtc payload"));
-    for (int i = 0; i < payload_count(); ++i) {
-        const char *n = nullptr, *s = nullptr;
-        payload_header(i, &n, &s);
-        h = fnv1a(n, h);
-        h = fnv1a(s, h);
+    for (int i = 0; i < kNumHeaders; ++i) {
+        h = fnv1a(kHeaders[i].name, h);
+        h = fnv1a(kHeaders[i].src, h);
+    }
+    return h;
+}
+
+uint64_t cache_key(const std::string& source, const std::string& arch, const std::string& tag, int nvrtc_major,
+                   int nvrtc_minor, int override_index, const char* override_src) {
+    const std::string opts_key =
+        arch + "|nvrtc" + std::to_string(nvrtc_major) + "." + std::to_string(nvrtc_minor) + "|" + tag;
+    uint64_t h = fnv1a(source);
+    h = fnv1a(opts_key, h);
+    for (int i = 0; i < kNumHeaders; ++i) {
+        h = fnv1a(kHeaders[i].name, h);
+        h = fnv1a(i == override_index && override_src ? override_src : kHeaders[i].src, h);
     }
     return h;
 }
 
 std::string compile_for_arch(const std::string& source, const std::string& arch) {
-    const char* hdr_src[] = {kAgDeviceSrc, kAgEmu64Src, kAgEmu64TablesSrc, kAgEmu64BmSrc, kAgEmu64BmTablesSrc};
-    const char* hdr_names[] = {"ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh", "ag_emu64_bm.cuh",
-                               "ag_emu64_bm_tables.cuh"};
+    const char* hdr_src[kNumHeaders];
+    const char* hdr_names[kNumHeaders];
+    for (int i = 0; i < kNumHeaders; ++i) {
+        hdr_src[i] = kHeaders[i].src;
+        hdr_names[i] = kHeaders[i].name;
+    }
     nvrtcProgram prog;
-    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_plan.cu", 5, hdr_src, hdr_names) != NVRTC_SUCCESS)
+    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_plan.cu", kNumHeaders, hdr_src, hdr_names) != NVRTC_SUCCESS)
         throw std::runtime_error("nvrtcCreateProgram failed");
     const std::string arch_opt = "--gpu-architecture=" + arch;
     const char* opts[] = {arch_opt.c_str(), "--std=c++17", "--fmad=true", "--dopt=on"};
@@ -132,12 +160,7 @@ Compiled compile_cached(const std::string& source, const std::string& tag) {
     const std::string arch = current_arch();
     int nvrtc_major = 0, nvrtc_minor = 0;
     nvrtcVersion(&nvrtc_major, &nvrtc_minor);
-    const std::string opts_key = arch + "|nvrtc" + std::to_string(nvrtc_major) + "." + std::to_string(nvrtc_minor) + "|" + tag;
-    uint64_t h = fnv1a(source);
-    h = fnv1a(opts_key, h);
-    h = fnv1a(kAgDeviceSrc, h);
-    h = fnv1a(kAgEmu64Src, h);
-    h = fnv1a(kAgEmu64TablesSrc, h);
+    const uint64_t h = cache_key(source, arch, tag, nvrtc_major, nvrtc_minor, -1, nullptr);
 
     Compiled out;
     out.hash = h;

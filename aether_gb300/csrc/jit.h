@@ -32,4 +32,12 @@ int payload_count();
 bool payload_header(int i, const char** name, const char** src);
 uint64_t payload_digest();
 
+// The cache key of `source` compiled for `arch` with option tag `tag` by
+// NVRTC major.minor: the source, the options and every payload header's name
+// and text. With override_index >= 0, header override_index is taken as
+// `override_src` instead of its embedded text (to show that a header edit
+// changes the key).
+uint64_t cache_key(const std::string& source, const std::string& arch, const std::string& tag, int nvrtc_major,
+                   int nvrtc_minor, int override_index, const char* override_src);
+
 }  // namespace ag

@@ -3,20 +3,22 @@
 // A sum plan needs device scratch: a completion counter plus one (hi, comp)
 // partial per chunk of samples. aether_plan_launch takes it from the caller
 // or allocates it for the plan on first use. Some callers cannot allocate at
-// the point where they launch: code recorded into a CUDA graph must not call
-// cudaMalloc, hosts that run under a fixed device-memory budget (a serving
-// loop that admits work by bytes) must not grow it behind their back, and
-// latency-critical loops cannot afford an allocation stall. For them,
-// aether_plan_launch_noalloc takes the scratch from a fixed array compiled
-// into this library instead.
+// the point where they launch: hosts that run under a fixed device-memory
+// budget (a serving loop that admits work by bytes) must not grow it behind
+// their back, and latency-critical loops cannot afford an allocation stall.
+// For them, aether_plan_launch_noalloc takes the scratch from a fixed array
+// compiled into this library instead.
 //
 // The array is a file-scope static __device__ buffer of AG_NOALLOC_SCRATCH_BYTES
 // (1 MiB) that every GPU which loads the library holds until the process
 // exits. Its device address is resolved once per device, on the first call
 // made with that device current (cudaGetSymbolAddress), so that first call
-// should come before any stream capture. All calls share the one array: the
-// counter is cleared at the start of every call, and calls whose kernels
-// overlap on the GPU (two streams, or two threads) race on it; serialise them.
+// should come before any stream capture; a first call on a capturing stream
+// is refused. The address is kept for the life of the process: after a
+// cudaDeviceReset the entry point is not usable, as plans are not. All calls
+// share the one array: the counter is cleared at the start of every call, and
+// calls whose kernels overlap on the GPU (two streams, or two threads) race
+// on it; serialise them.
 
 #include <cuda_runtime.h>
 
@@ -62,6 +64,15 @@ extern "C" __attribute__((visibility("default"))) int aether_plan_launch_noalloc
     {
         std::lock_guard<std::mutex> lk(g_mu);
         if (!g_addr[dev]) {
+            // resolving the symbol may load the module; never do that inside
+            // a caller's capture
+            cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+            e = cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &st);
+            if (e != cudaSuccess)
+                return fail_msg(std::string("plan_launch_noalloc: cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+            if (st != cudaStreamCaptureStatusNone)
+                return fail_msg("plan_launch_noalloc: the first call on a device must come before any stream "
+                                "capture (it resolves the static scratch's address); make one uncaptured call first");
             e = cudaGetSymbolAddress(&g_addr[dev], g_noalloc_scratch);
             if (e != cudaSuccess) {
                 g_addr[dev] = nullptr;

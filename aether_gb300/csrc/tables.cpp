@@ -70,6 +70,7 @@ const AetherGB300V1 kGB300 = {
     aether_rtc_digest,
     aether_plan_generate,
     aether_nvrtc_check,
+    aether_plan_cache_key,
 };
 
 }  // namespace

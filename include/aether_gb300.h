@@ -100,7 +100,15 @@ typedef struct AetherLaunch {
     const uint64_t* keys;         /* Generator keys of random leaves (random/Generator.h:183) */
     uint32_t n_keys;
     double* reduce_out;           /* sum plans: device pointer to (hi, comp) */
-    void* workspace;              /* sum plans: device scratch, or NULL for the plan's own */
+    /* Sum plans: device scratch of aether_plan_workspace_size bytes, or NULL
+     * for one of the plan's own. Own workspaces form a pool: a launch reuses
+     * an entry last used on the same stream or one whose last launch has
+     * finished, and allocates a new entry otherwise, so concurrent launches
+     * of one plan on different streams never share scratch. A caller-given
+     * workspace is the caller's to keep private to one launch at a time. A
+     * launch recorded into a CUDA graph needs a caller-given workspace (or
+     * aether_plan_launch_noalloc); without one it is refused. */
+    void* workspace;
     uint64_t workspace_bytes;
 } AetherLaunch;
 
@@ -110,7 +118,9 @@ typedef struct AetherLowering {
     int ipt;          /* lane groups per thread per chunk */
     int vec;          /* samples per lane group (vector width) */
     int contract;     /* 1: FMA contraction allowed, 0: every add/mul rounds (-fmad=false), -1: default (1) */
-    int math;         /* 0: FP64 on the FP64 pipe; 1: FP64 emulated on the FP32/INT pipes */
+    int math;         /* 0: FP64 on the FP64 pipe; 1: FP64 emulated on the FP32/INT pipes (double-float);
+                         2: the precision form -- f32 or float-float storage evaluated in double-float
+                         arithmetic, exact products of f32 operands, FP64 only in the final stage of sums */
     int min_blocks;   /* __launch_bounds__ min blocks per SM */
 } AetherLowering;
 
@@ -181,15 +191,17 @@ int aether_plan_launch_many(void* const* plans, const AetherLaunch* args, int co
 
 /* Launch a sum plan without allocating anything on the device. No counterpart
  * in the reference: it exists for callers that cannot call cudaMalloc where
- * they launch -- work being recorded into a CUDA graph, hosts that run under a
- * fixed device-memory budget, latency-critical loops. The plan's scratch (a
- * counter and one partial per chunk, 16 + 16 * chunks bytes) comes from a
- * 1 MiB array compiled into the library that every GPU which loads it holds
- * until exit; sizes that need more are refused with an error naming the
- * limit. `args->workspace` must be NULL. The first call on a device resolves
- * the array's address and should come before any stream capture. Calls share
- * the array (the counter is cleared at each call), so calls whose kernels
- * overlap on the GPU race and must be serialised by the caller. */
+ * they launch -- hosts that run under a fixed device-memory budget,
+ * latency-critical loops. The plan's scratch (a counter and one partial per
+ * chunk, 16 + 16 * chunks bytes) comes from a 1 MiB array compiled into the
+ * library that every GPU which loads it holds until exit; sizes that need more
+ * are refused with an error naming the limit. `args->workspace` must be NULL.
+ * The first call on a device resolves the array's address and should come
+ * before any stream capture (a first call on a capturing stream is refused);
+ * the address is kept for the process, so the entry point is not usable after
+ * a cudaDeviceReset. Calls share the array (the counter is cleared at each
+ * call), so calls whose kernels overlap on the GPU race and must be
+ * serialised by the caller. */
 int aether_plan_launch_noalloc(void* plan, const AetherLaunch* args, void* stream);
 
 /* ------------------------------------------------------------------------- *
@@ -342,6 +354,16 @@ int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* b
 int aether_rtc_header_count(void);
 int aether_rtc_header(int index, const char** name, const char** source);
 uint64_t aether_rtc_digest(void);
+/* The in-memory and on-disk cache key of a generated kernel: `source` compiled
+ * for `arch` under option tag `tag` by this library's NVRTC, hashed with the
+ * name and text of every payload header above, so a kernel cached before any
+ * of those headers changed is never served after the change. With
+ * header_index >= 0 the key is computed as if payload header `header_index`
+ * held `header_source` instead (no device needed; used to check that every
+ * header reaches the key). No counterpart in the reference, which compiles
+ * consumer kernels ahead of time with nvcc. */
+int aether_plan_cache_key(const char* source, const char* arch, const char* tag, int header_index,
+                          const char* header_source, uint64_t* key);
 /* Compile `source` with NVRTC for `arch` (e.g. "sm_103a") without loading it;
  * on failure the compiler log is the last error. */
 int aether_nvrtc_check(const char* source, const char* arch);
@@ -416,6 +438,8 @@ typedef struct AetherGB300V1 {
     uint64_t (*rtc_digest)(void);
     int (*plan_generate)(const char* ir, const AetherLowering* lowering, char* buf, size_t cap, size_t* len);
     int (*nvrtc_check)(const char* source, const char* arch);
+    int (*plan_cache_key)(const char* source, const char* arch, const char* tag, int header_index,
+                          const char* header_source, uint64_t* key);
 } AetherGB300V1;
 const AetherGB300V1* aether_gb300_v1(void);
 

@@ -75,8 +75,11 @@ def run_reference(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("AETHER_REFERENCE_DIR"),
+                    help="checkout of the reference (default: $AETHER_REFERENCE_DIR)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("name the reference checkout with --ref or AETHER_REFERENCE_DIR")
     g = parse_golden_random(os.path.join(args.ref, "tests", "random", "golden_random.h"))
     with open(os.path.join(HERE, "philox_golden.json"), "w") as f:
         json.dump(g, f, indent=0)

@@ -193,7 +193,7 @@ def test_gb300_table_binds_every_path_entry():
              "batch_set_items", "batch_launch", "batch_capture", "batch_replay", "batch_info", "batch_release",
              "serve_open", "serve_submit", "serve_feed", "serve_status", "serve_wait", "serve_release", "serve_stats",
              "serve_close", "runtime_eval", "rtc_header_count", "rtc_header", "rtc_digest", "plan_generate",
-             "nvrtc_check"]
+             "nvrtc_check", "plan_cache_key"]
 
     class T(ctypes.Structure):
         _fields_ = [("abi", ctypes.c_uint32), ("memory", P)] + [(n, P) for n in names]
@@ -202,3 +202,49 @@ def test_gb300_table_binds_every_path_entry():
     assert t.abi == 1 and t.memory == L.aether_memory_v1()
     for n in names:
         assert getattr(t, n) == ctypes.cast(getattr(L, "aether_" + n), P).value, n
+
+
+def test_cache_key_covers_every_payload_header():
+    # A kernel cached on disk must never be served after any header it may
+    # include changes: flipping one byte of any payload header (the
+    # Box-Muller headers included) gives a new key.
+    from aether_gb300 import _abi
+    L = _abi.lib()
+
+    def key(idx=-1, src=None):
+        k = ctypes.c_uint64()
+        _abi.check(L.aether_plan_cache_key(b"extern \"C\" __global__ void k() {}", b"sm_103a", b"plan", idx, src,
+                                           ctypes.byref(k)))
+        return k.value
+
+    base = key()
+    assert key() == base
+    n = L.aether_rtc_header_count()
+    assert n >= 5
+    seen = {base}
+    for i in range(n):
+        name = ctypes.c_char_p()
+        text = ctypes.c_char_p()
+        _abi.check(L.aether_rtc_header(i, ctypes.byref(name), ctypes.byref(text)))
+        assert key(i, text.value) == base, name.value     # the same text: the same key
+        edited = bytearray(text.value)
+        edited[len(edited) // 2] ^= 1
+        k = key(i, bytes(edited))
+        assert k not in seen, name.value
+        seen.add(k)
+    assert L.aether_plan_cache_key(b"x", b"sm_103a", b"plan", n, b"", ctypes.byref(ctypes.c_uint64())) == 1
+
+
+def test_plugin_library_exports_exactly_the_seam_table():
+    # libaether_cuda.so is the drop-in for the reference's CUDA plugin: one
+    # exported symbol, aether_memory_v1, as dsc/src/plugin.map declares
+    import subprocess
+    from aether_gb300 import _abi, build
+    _abi.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", build.PLUGIN], capture_output=True, text=True).stdout
+    funcs = sorted(l.split()[-1] for l in out.splitlines() if l.split() and l.split()[-2] in ("T", "D", "R", "B"))
+    assert funcs == ["aether_memory_v1"], funcs
+    P = ctypes.CDLL(build.PLUGIN)
+    P.aether_memory_v1.restype = ctypes.c_void_p
+    abi = ctypes.cast(P.aether_memory_v1(), ctypes.POINTER(ctypes.c_uint32)).contents.value
+    assert abi == 2

@@ -1,8 +1,9 @@
 """aether_plan_launch_noalloc: a sum plan launched with the library's static
 scratch instead of an allocation, for callers that cannot call cudaMalloc
-where they launch (graph capture, fixed device-memory budgets, latency
-loops). Checked through the C-ABI against aether_plan_launch on the same
-plan, on two calls in a row. This file is collected last on purpose."""
+where they launch (fixed device-memory budgets, latency loops). Checked
+through the C-ABI against aether_plan_launch on the same plan, on two calls in
+a row, at the largest size the scratch holds and one chunk beyond it. This
+file is collected last on purpose."""
 
 import ctypes
 
@@ -44,8 +45,7 @@ def _launch_args(ag, x, y, n, out):
 IR = "(plan f64 [] sum (dot (in 0 f64 [8]) (in 1 f64 [8])))"
 
 
-def test_noalloc_sum_matches_plan_launch_on_two_calls():
-    n = 300001
+def _check_two_calls(n):
     ag, x, y = _setup(n)
     L = ag._abi.lib()
     plan = ag.get_plan(IR)
@@ -65,6 +65,43 @@ def test_noalloc_sum_matches_plan_launch_on_two_calls():
         # same kernel, same chunk tree: the compensated sums agree to the
         # tolerance of the other sum tests (and in practice bit for bit)
         assert abs((got[0] + got[1]) - (r[0] + r[1])) <= 4e-16 * absmag
+
+
+def test_noalloc_sum_matches_plan_launch_on_two_calls():
+    _check_two_calls(300001)
+
+
+def _largest_accepted(ag, plan):
+    # the scratch need grows by 16 bytes per chunk of samples: find the
+    # largest n whose need fits the 1 MiB array
+    L = ag._abi.lib()
+
+    def need(n):
+        b = ctypes.c_uint64()
+        ag._abi.check(L.aether_plan_workspace_size(plan.handle, n, ctypes.byref(b)))
+        return b.value
+
+    lo, hi = 1, 1 << 31
+    assert need(lo) <= 1 << 20 < need(hi)
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        lo, hi = (mid, hi) if need(mid) <= 1 << 20 else (lo, mid)
+    return lo
+
+
+def test_noalloc_edge_of_the_scratch():
+    import aether_gb300 as ag
+    L = ag._abi.lib()
+    plan = ag.get_plan(IR)
+    n_max = _largest_accepted(ag, plan)
+    _check_two_calls(n_max)
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    a = ag._abi.AetherLaunch()
+    a.n = n_max + 1   # one chunk more than the scratch holds
+    a.reduce_out = out.data_ptr()
+    rc = L.aether_plan_launch_noalloc(plan.handle, ctypes.byref(a), None)
+    assert rc == 1
+    assert b"static scratch holds" in L.aether_last_error()
 
 
 def test_noalloc_refuses_sizes_beyond_its_scratch():
