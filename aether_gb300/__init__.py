@@ -232,6 +232,13 @@ class Plan:
         _abi.check(_abi.lib().aether_plan_source(self.handle, buf, n.value + 1, ctypes.byref(n)))
         return buf.value.decode()
 
+    @property
+    def name(self):
+        """The kernel's base name (its vectorised and scalar kernels add _v / _s)."""
+        import re
+        m = re.search(r"\b(ag_(?:expr|fill|sum)_[0-9a-f]{8})_v\b", self.source())
+        return m.group(1) if m else None
+
     def workspace_size(self, n):
         b = ctypes.c_uint64()
         _abi.check(_abi.lib().aether_plan_workspace_size(self.handle, n, ctypes.byref(b)))

@@ -27,9 +27,12 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["plan.cpp", "jit.cpp", "abi.cpp", "serve.cpp", "tables.cpp"]
 DEVICE_SOURCES = ["noalloc.cu", "runtime.cu", "serve_copy.cu"]
-EMBED = [("kAgDeviceSrc", "device/ag_device.cuh"), ("kAgEmu64Src", "device/ag_emu64.cuh"),
-         ("kAgEmu64TablesSrc", "device/ag_emu64_tables.cuh"), ("kAgEmu64BmSrc", "device/ag_emu64_bm.cuh"),
-         ("kAgEmu64BmTablesSrc", "device/ag_emu64_bm_tables.cuh")]
+# The device runtime headers live in the public include tree (consumer kernels
+# compiled with nvcc include them too); generated kernels get them embedded.
+DEVICE_INC = os.path.join(REPO, "include", "aether", "gb300")
+EMBED = [("kAgDeviceSrc", "ag_device.cuh"), ("kAgEmu64Src", "ag_emu64.cuh"),
+         ("kAgEmu64TablesSrc", "ag_emu64_tables.cuh"), ("kAgEmu64BmSrc", "ag_emu64_bm.cuh"),
+         ("kAgEmu64BmTablesSrc", "ag_emu64_bm_tables.cuh")]
 EXPORT_PREFIX = "aether_"
 
 
@@ -51,9 +54,9 @@ def _write_if_changed(path, text):
 
 
 def _embed():
-    parts = ["// generated by aether_gb300/build.py from csrc/device/*.cuh\n"]
+    parts = ["// generated by aether_gb300/build.py from include/aether/gb300/*.cuh\n"]
     for name, rel in EMBED:
-        src = open(os.path.join(CSRC, rel)).read()
+        src = open(os.path.join(DEVICE_INC, rel)).read()
         delim = "AGSRC"
         assert ")" + delim + '"' not in src
         # Raw literals are limited in length by some compilers: split in pieces.
@@ -78,8 +81,9 @@ def _stale(obj, deps):
 
 def _headers():
     out = []
-    for root, _, files in os.walk(CSRC):
-        out += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh", ".inc"))]
+    for top in (CSRC, os.path.join(REPO, "include", "aether")):
+        for root, _, files in os.walk(top):
+            out += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh", ".inc"))]
     out.append(os.path.join(REPO, "include", "aether_gb300.h"))
     out.append(os.path.join(BUILD, "embedded.inc"))
     return out
@@ -91,7 +95,8 @@ def build(force=False, verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     _embed()
     _exports()
-    inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC, "-I" + BUILD, "-I" + os.path.join(cuda, "include")]
+    inc = ["-I" + os.path.join(REPO, "include"), "-I" + DEVICE_INC, "-I" + CSRC, "-I" + BUILD,
+           "-I" + os.path.join(cuda, "include")]
     hdrs = _headers()
     jobs = []
     objs = []

@@ -25,7 +25,7 @@
 #include <string>
 
 #include "aether_gb300.h"
-#include "device/ag_fastdiv.cuh"
+#include "ag_fastdiv.cuh"
 
 int ag_internal_fail(const char* message);
 

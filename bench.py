@@ -48,17 +48,20 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """dram bytes per sample of the expression kernel from the committed ncu
-    summary (profiles/), or None."""
+def profile_figures():
+    """Per-kernel figures from the committed ncu summaries (profiles/ncu_traffic.txt):
+    {kind: {"kernel": name, "bytes_per_sample": B, "inst_per_sample": I}}. Each
+    line reads `<kind> <kernel name> <dram bytes/sample> <thread instructions/sample>`."""
     path = os.path.join(REPO, "profiles", "ncu_traffic.txt")
+    out = {}
     try:
         for line in open(path):
-            if line.startswith("expr_bytes_per_sample:"):
-                return float(line.split(":")[1])
-    except Exception:
+            f = line.split()
+            if len(f) == 4 and not line.startswith("#"):
+                out[f[0]] = {"kernel": f[1], "bytes_per_sample": float(f[2]), "inst_per_sample": float(f[3])}
+    except OSError:
         pass
-    return None
+    return out
 
 
 class ClockSampler:
@@ -150,22 +153,35 @@ def cpu_leg(steps, warmup, nthreads=0, expr_samples=1 << 23, fill_samples=1 << 2
     return gbs, t, nt, sample, (ins, d_out, z_out)
 
 
-def check_against_oracle(arrs, d, z, ins, d_ref, z_ref):
+def check_against_oracle(arrs, d, z, ins, d_ref, z_ref, math):
     """The GPU step's results on the CPU leg's sample against the oracle's
     (same seeded inputs): inputs bit for bit, the expression in units of
-    2^-53 of its term scale, the normals in the reference's abs+rel form."""
+    2^-53 of its term scale, the normals in the reference's abs+rel form,
+    each against the stated bound of the lowering (aether_gb300.accuracy)."""
     import numpy as np
+    from aether_gb300 import accuracy as acc
     n, nz = d_ref.shape[1], z_ref.shape[1]
     same_inputs = all(np.array_equal(x.data[:, :n].cpu().numpy(), r[:, :n]) for x, r in zip(arrs, ins))
     got = d.data[:, :n].cpu().numpy()
     a, b, c, d0 = (r[:, :n] for r in ins)
     scale = np.maximum(np.abs(np.sqrt(a * a + b * b) * np.log1p(np.abs(c))), np.abs(1.0 / np.sqrt(1.0 + d0 * d0)))
-    e_expr = float(np.max(np.abs(got - d_ref[:, :n]) / scale)) / 2.0 ** -53
-    gz = z.data[:, :nz].cpu().numpy()
-    e_norm = float(np.max(np.abs(gz - z_ref[:, :nz]) / (1.0 + np.abs(z_ref[:, :nz])))) / 2.0 ** -53
-    return {"inputs_bit_exact": bool(same_inputs), "expr_samples": int(n), "expr_max_err_2m53_of_terms": round(e_expr, 1),
-            "normal_samples": int(nz), "normal_max_err_2m53_abs_rel": round(e_norm, 1),
-            "expr_bound_2m53": 512, "normal_bound_2m53": 256, "reference_normal_tol": 1e-12}
+    e_expr = acc.term_scale_error_2m53(got, d_ref[:, :n], scale)
+    e_norm = acc.abs_rel_error_2m53(z.data[:, :nz].cpu().numpy(), z_ref[:, :nz])
+    out = {"lowering": ["native FP64", "emulated FP64"][math], "inputs_bit_exact": bool(same_inputs),
+           "expr_samples": int(n), "expr_max_err_2m53_of_terms": round(e_expr, 2),
+           "normal_samples": int(nz), "normal_max_err_2m53_abs_rel": round(e_norm, 2), "reference_normal_tol": 1e-12}
+    if math == 0:
+        # native: ulp of the largest term, the unit the native bound is stated in
+        e_ulp = acc.term_scale_error_ulp(got, d_ref[:, :n], scale)
+        out.update({"expr_max_err_ulp_of_terms": round(e_ulp, 2), "expr_bound_ulp_of_terms": acc.NATIVE_EXPR_ULPS,
+                    "normal_bound_2m53": acc.NATIVE_NORMAL_BOUND_2M53,
+                    "within_bounds": bool(same_inputs and e_ulp <= acc.NATIVE_EXPR_ULPS and
+                                          e_norm <= acc.NATIVE_NORMAL_BOUND_2M53)})
+    else:
+        out.update({"expr_bound_2m53": acc.EMU_EXPR_BOUND_2M53, "normal_bound_2m53": acc.EMU_NORMAL_BOUND_2M53,
+                    "within_bounds": bool(same_inputs and e_expr <= acc.EMU_EXPR_BOUND_2M53 and
+                                          e_norm <= acc.EMU_NORMAL_BOUND_2M53)})
+    return out
 
 
 def run_reference(args):
@@ -484,6 +500,87 @@ def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, satu
     return res
 
 
+def time_steps(k_expr, k_fill, steps, stream):
+    """`steps` back-to-back steps with events around each kernel on the
+    launching stream: (total ms, [expression ms], [fill ms])."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for i in range(steps):
+        ev[i][0].record(stream)
+        k_expr()
+        ev[i][1].record(stream)
+        k_fill()
+        ev[i][2].record(stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    return (start.elapsed_time(end), [e[0].elapsed_time(e[1]) for e in ev], [e[1].elapsed_time(e[2]) for e in ev])
+
+
+def l2_twin_gbs(launch, samples, bytes_per_sample, reps=40):
+    """The same kernel on an L2-resident slice (its working set well inside
+    the 129 MB L2), back to back: the rate the kernel reaches when HBM is not
+    what limits it, i.e. its compute ceiling, in the same algorithmic bytes."""
+    ms = _time_ms(launch, reps=reps, warmup=3)
+    return samples * bytes_per_sample / (ms * 1e-3) / 1e9
+
+
+def kernel_roofline(name, kernel, nbytes, ms, peak, twin_gbs, prof, samples, clock_mhz, sms):
+    """One kernel's roofline entry: HBM fraction of the measured copy peak;
+    the issue ceiling (the profiled thread instructions per sample at SMs x 4
+    schedulers x 32 lanes x the sampled clock) and the DRAM traffic of the
+    committed capture when it is of this very kernel; the rate of the same
+    kernel on an L2-resident slice when one was timed; and the bound: the
+    lower of the HBM and issue ceilings."""
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    e = {"kernel": kernel, "bytes_per_launch": nbytes, "ms": round(ms, 4), "achieved": round(achieved, 2),
+         "frac": round(achieved / peak, 4)}
+    if twin_gbs:
+        e["l2_resident_gbs"] = round(twin_gbs, 1)
+    p = prof.get(name)
+    e["bound"] = "hbm"
+    if p and p["kernel"] == kernel:
+        e["traffic"] = round(p["bytes_per_sample"] * samples)
+        if clock_mhz:
+            issue_ms = p["inst_per_sample"] * samples / (sms * 4 * 32 * clock_mhz * 1e6) * 1e3
+            issue_gbs = nbytes / (issue_ms * 1e-3) / 1e9
+            e["inst_per_sample"] = p["inst_per_sample"]
+            e["issue_roof_gbs"] = round(issue_gbs, 1)
+            e["frac_of_issue_roof"] = round(achieved / issue_gbs, 4)
+            e["bound"] = "issue" if issue_gbs < peak else "hbm"
+    else:
+        e["traffic"] = None
+        e["traffic_note"] = ("no committed ncu capture of this kernel" if not p else
+                             "committed capture is of %s, not of the kernel that ran" % p["kernel"])
+    return e
+
+
+def native_fp64_step(ag, arrs, d, z, expr, g, steps, stream, ref):
+    """The same step lowered to native FP64 (math 0: CUDA's FP64 functions on
+    the FP64 pipe, the reference's own precision), timed like the headline
+    and checked against the oracle on the CPU leg's slice."""
+    k_expr = ag.prepare(d, expr, math=0, tune=True)
+    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=0, tune=True)
+    for _ in range(2):
+        k_expr()
+        k_fill()
+    total, te, tf = time_steps(k_expr, k_fill, max(3, min(steps, 5)), stream)
+    te, tf = statistics.mean(te), statistics.mean(tf)
+    peak, _ = peaks()
+    n_steps = max(3, min(steps, 5))
+    out = {"ms_per_step": round(total / n_steps, 4),
+           "value": round((BYTES_EXPR + BYTES_FILL) / (total / n_steps * 1e-3) / 1e9, 2),
+           "expr": {"kernel": k_expr.plan.name, "ms": round(te, 4), "gbs": round(BYTES_EXPR / (te * 1e-3) / 1e9, 1),
+                    "frac": round(BYTES_EXPR / (te * 1e-3) / 1e9 / peak, 4)},
+           "fill": {"kernel": k_fill.plan.name, "ms": round(tf, 4), "gbs": round(BYTES_FILL / (tf * 1e-3) / 1e9, 1),
+                    "frac": round(BYTES_FILL / (tf * 1e-3) / 1e9 / peak, 4)}}
+    if ref is not None:
+        out["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref, math=0)
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -518,23 +615,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         time.sleep(0.3)
-        start.record(stream)
-        for i in range(args.steps):
-            ev[i][0].record(stream)
-            k_expr()
-            ev[i][1].record(stream)
-            k_fill()
-            ev[i][2].record(stream)
-        end.record(stream)
-        torch.cuda.synchronize()
-    total_ms = start.elapsed_time(end)
-    t_expr = [e[0].elapsed_time(e[1]) for e in ev]
-    t_fill = [e[1].elapsed_time(e[2]) for e in ev]
+        total_ms, t_expr, t_fill = time_steps(k_expr, k_fill, args.steps, stream)
     total_ms = shard.max_over_ranks(total_ms, group=dist.group.WORLD if dist else None)
     ms_step = total_ms / args.steps
     value = ws * (BYTES_EXPR + BYTES_FILL) / (ms_step * 1e-3) / 1e9
@@ -657,24 +740,49 @@ def run_ours(args):
     peak, peak_kind = peaks()
     te = statistics.mean(t_expr)
     tf = statistics.mean(t_fill)
-    achieved = BYTES_EXPR / (te * 1e-3) / 1e9
-    tr = profile_traffic()
-    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "traffic": round(tr * N_EXPR) if tr else None,
-                "kernel": "expression (a) sqrt/log1p/rsqrt plan", "kernel_ms": round(te, 4),
-                "fill_ms": round(tf, 4), "fill_gbs": round(BYTES_FILL / (tf * 1e-3) / 1e9, 2),
-                "fill_frac": round(BYTES_FILL / (tf * 1e-3) / 1e9 / peak, 4)}
+    clocks = clk.summary()
+    props = torch.cuda.get_device_properties(local)
+    prof = profile_figures()
+    # the write-only fill fits a 2^23-double (64 MB) slice in L2 with enough
+    # chunks to fill every SM; the expression's 120 B/sample does not, so its
+    # compute ceiling is the issue ceiling alone
+    n_tw_f = min(N_FILL, 1 << 23)
+    twin_e = None
+    twin_f = l2_twin_gbs(ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), n=n_tw_f, math=math_mode,
+                                    tune=not args.no_tune), n_tw_f, 8)
+    kernels = {
+        "expr": kernel_roofline("expr", k_expr.plan.name + "_v", BYTES_EXPR, te, peak, twin_e, prof, N_EXPR,
+                                clocks.get("sm_mhz"), props.multi_processor_count),
+        "fill": kernel_roofline("fill", k_fill.plan.name + "_v", BYTES_FILL, tf, peak, twin_f, prof, N_FILL,
+                                clocks.get("sm_mhz"), props.multi_processor_count),
+    }
+    dom = "fill" if tf >= te else "expr"
+    k = kernels[dom]
+    roofline = {"bound": "hbm", "achieved": k["achieved"], "peak": peak, "unit": "GB/s", "frac": k["frac"],
+                "peak_kind": peak_kind, "traffic": k["traffic"],
+                "kernel": dom + ": " + k["kernel"] + " (the larger share of the step)",
+                "share_of_step": round(max(te, tf) / (te + tf), 3), "binding_roof": k["bound"],
+                "issue_roof_gbs": k.get("issue_roof_gbs"), "frac_of_issue_roof": k.get("frac_of_issue_roof"),
+                "kernels": kernels,
+                "issue_roof": "profiled thread instructions per sample (profiles/ncu_traffic.txt) at SMs x 4 "
+                              "schedulers x 32 lanes x the sampled SM clock; l2_resident_gbs: the fill timed on "
+                              "a 2^23-double slice that stays in L2"}
     cpu = None
+    ref = None
     if not args.no_cpu:
         gbs, t, nt, sample, ref = cpu_leg(1, 1)
         cpu = {"value": round(gbs, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample}
         # the oracle doubles as the checker of this run's GPU results
-        cpu["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref)
+        cpu["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref, math=math_mode)
     secondary = None
     if not args.no_secondary:
         # the other configurations, measured after the timed region
         secondary = {}
+        if math_mode != 0:
+            try:
+                secondary["native_fp64_step"] = native_fp64_step(ag, arrs, d, z, expr, g, args.steps, stream, ref)
+            except Exception as ex:   # reported, never hidden
+                secondary["native_fp64_step"] = {"error": str(ex).splitlines()[0][:300] if str(ex) else repr(ex)}
         for name, fn in (("config1_plain", secondary_config1), ("config3_precision_form", secondary_config3),
                          ("config4_batch", secondary_config4), ("config5_serving", secondary_config5)):
             try:
@@ -693,7 +801,7 @@ def run_ours(args):
                                      "vec": k_fill.plan.info().vec, "registers": k_fill.plan.info().registers},
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": 2 * args.steps, "clocks": clk.summary(), "secondary": secondary,
+        "gpu_launches": 2 * args.steps, "clocks": clocks, "secondary": secondary,
     }
     print(json.dumps(line), flush=True)
     if dist:

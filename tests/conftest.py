@@ -74,3 +74,11 @@ def assert_ulp(got, ref, ulps, scale=None, what=""):
         raise AssertionError("%s: %d values beyond %g ulp; first at %s: got %r ref %r (err %g, bound %g)"
                              % (what, bad.sum(), ulps, tuple(i), got[tuple(i)], ref[tuple(i)], err[tuple(i)],
                                 bound[tuple(i)]))
+
+
+def assert_term_scale(got, ref, bound_2m53, scale, what=""):
+    """|got - ref| <= bound_2m53 * 2^-53 * scale, scale the largest term's
+    magnitude (the unit of aether_gb300.accuracy's emulated bounds)."""
+    from aether_gb300.accuracy import term_scale_error_2m53
+    e = term_scale_error_2m53(got, ref, scale)
+    assert e <= bound_2m53, "%s: %.1f x 2^-53 of the term scale, bound %d" % (what, e, bound_2m53)

@@ -1,12 +1,12 @@
 // Host check of the invariant-divisor division the strided runtime kernels
-// use (aether_gb300/csrc/device/ag_fastdiv.cuh) against the hardware divide:
+// use (include/aether/gb300/ag_fastdiv.cuh) against the hardware divide:
 // every divisor up to 4096 on edge and random dividends, then random and
 // edge divisor/dividend pairs over the whole 32-bit range.
 #include <cstdint>
 #include <cstdio>
 #include <random>
 
-#include "device/ag_fastdiv.cuh"
+#include "aether/gb300/ag_fastdiv.cuh"
 
 static int check(uint32_t x, uint32_t d) {
     const AgFastDiv f = ag_fastdiv_make(d);

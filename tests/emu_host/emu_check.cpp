@@ -3,8 +3,8 @@
 // relative error in units of 2^-53 over a seeded corpus. Test infrastructure.
 #include "host_shim.h"
 
-#include "../../aether_gb300/csrc/device/ag_emu64.cuh"
-#include "../../aether_gb300/csrc/device/ag_emu64_bm.cuh"
+#include "../../include/aether/gb300/ag_emu64.cuh"
+#include "../../include/aether/gb300/ag_emu64_bm.cuh"
 
 #include <cstdio>
 #include <random>

@@ -1,5 +1,5 @@
 // host_shim.h -- host spellings of the CUDA intrinsics that
-// aether_gb300/csrc/device/ag_emu64.cuh uses, so the double-float algorithms
+// include/aether/gb300/ag_emu64.cuh uses, so the double-float algorithms
 // can be compiled as host C++ and checked against long double. Test
 // infrastructure only (compiled with -ffp-contract=off: every _rn operation
 // rounds once, as on the device).

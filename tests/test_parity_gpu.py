@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import assert_ulp, ulp_diff
+from conftest import assert_term_scale, assert_ulp, ulp_diff
 
 pytestmark = pytest.mark.gpu
 
@@ -28,6 +28,7 @@ def _gpu():
 
 
 import aether_gb300 as ag
+from aether_gb300.accuracy import EMU_EXPR_BOUND_2M53, EMU_NORMAL_BOUND_2M53, NATIVE_EXPR_ULPS
 
 ULP_F64 = {"exp": 2, "log": 2, "log1p": 2, "expm1": 2, "sin": 3, "cos": 3, "tan": 3, "asin": 3, "acos": 3,
            "atan": 3, "tanh": 2, "pow": 3, "sqrt": 0, "rsqrt": 0, "div": 0}
@@ -160,9 +161,11 @@ def test_config1_full_size(oracle):
     assert_ulp(d.host(), ref, 4, scale, "config 1, 2^20 samples")
 
 
-# Emulated FP64 (math=1): double-float arithmetic, relative error ~2^-45 of
-# the largest term (tests/test_emu64_host.py derives the per-function bounds).
-EMU_ULPS = 256
+# Emulated FP64 (math=1): double-float arithmetic; the stated bounds live in
+# aether_gb300.accuracy (tests/test_emu64_host.py derives the per-function
+# bounds on the host).
+EMU_BOUND = EMU_EXPR_BOUND_2M53
+EMU_ULPS = 256   # emulated against native FP64 where both are in range
 
 
 @pytest.mark.parametrize("math", [0, 1])
@@ -173,7 +176,10 @@ def test_config2a_parity(oracle, ref_cases, math):
     ag.assign(d, _cfg2a(*(x.view() for x in ins)), math=math)
     A, B, C, D0 = (z[k] for k in ("cfg2a_a", "cfg2a_b", "cfg2a_c", "cfg2a_d0"))
     scale = np.maximum(np.abs(np.sqrt(A * A + B * B) * np.log1p(np.abs(C))), np.abs(1 / np.sqrt(1 + D0 * D0)))
-    assert_ulp(d.host(), z["cfg2a_d"], 4 if math == 0 else EMU_ULPS, scale, "config 2a vs reference")
+    if math == 0:
+        assert_ulp(d.host(), z["cfg2a_d"], NATIVE_EXPR_ULPS, scale, "config 2a vs reference")
+    else:
+        assert_term_scale(d.host(), z["cfg2a_d"], EMU_BOUND, scale, "config 2a emulated vs reference")
 
 
 def test_config2a_emulated_full_size_subsample(oracle):
@@ -188,7 +194,7 @@ def test_config2a_emulated_full_size_subsample(oracle):
     ref = oracle.cfg2a(*sub)
     A, B, C, D0 = sub
     scale = np.maximum(np.abs(np.sqrt(A * A + B * B) * np.log1p(np.abs(C))), np.abs(1 / np.sqrt(1 + D0 * D0)))
-    assert_ulp(d.data[:, idx].cpu().numpy(), ref, EMU_ULPS, scale, "config 2a emulated, 2^24 samples")
+    assert_term_scale(d.data[:, idx].cpu().numpy(), ref, EMU_BOUND, scale, "config 2a emulated, 2^24 samples")
 
 
 def test_config1_emulated(oracle, ref_cases):
@@ -198,7 +204,7 @@ def test_config1_emulated(oracle, ref_cases):
     ag.assign(d, _cfg1(a.view(), b.view(), c.view()), math=1)
     A, B, C = z["cfg1_a"], z["cfg1_b"], z["cfg1_c"]
     scale = np.maximum.reduce([np.abs(A), np.abs(B * C), np.abs(np.sin(A) * np.exp(-C * C))])
-    assert_ulp(d.host(), z["cfg1_d"], EMU_ULPS, scale, "config 1 emulated vs reference")
+    assert_term_scale(d.host(), z["cfg1_d"], EMU_BOUND, scale, "config 1 emulated vs reference")
 
 
 def test_emulated_uniform_fill_is_bit_exact(oracle):
@@ -217,8 +223,8 @@ def test_emulated_normal_fill_within_reference_tolerance(oracle):
     ag.assign(y, ag.Generator(7).substream(4).normal(1, 0.0, 1.0), math=1)
     r = oracle.fill_normal_f64(ag.Generator(7).substream(4).key, 0.0, 1.0, 1, n)
     err = np.abs(y.host() - r) / (1 + np.abs(r))
-    assert err.max() <= 256 * 2.0 ** -53, err.max() / 2.0 ** -53
-    assert err[0, 18695431] <= 256 * 2.0 ** -53
+    assert err.max() <= EMU_NORMAL_BOUND_2M53 * 2.0 ** -53, err.max() / 2.0 ** -53
+    assert err[0, 18695431] <= EMU_NORMAL_BOUND_2M53 * 2.0 ** -53
 
 
 def test_emulated_fallback_reproduces_native_on_special_inputs():
