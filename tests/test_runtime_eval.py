@@ -208,7 +208,7 @@ def test_fastdiv_matches_hardware_divide(tmp_path):
         pytest.skip("no host C++ compiler")
     repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     exe = str(tmp_path / "fastdiv_check")
-    subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(repo, "aether_gb300", "csrc"),
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(repo, "include"),
                     os.path.join(repo, "tests", "cpp", "fastdiv_check.cpp"), "-o", exe], check=True)
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0 and "fastdiv ok" in r.stdout, r.stdout
