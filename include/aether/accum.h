@@ -23,9 +23,11 @@ class Plane {
 public:
     explicit Plane(std::size_t n) : store_(n) { zero(); }
 
-    View<double, VD> value() { return View<double, VD>(store_.deviceView().data(), store_.capacity(), store_.samples()); }
-    View<double, VD> compensation() {
-        return View<double, VD>(store_.deviceView().data() + VD * store_.capacity(), store_.capacity(), store_.samples());
+    using PlaneView = View<double, extents<VD, dyn>, layout_stride>;
+    PlaneView value() { return detail::plane_view<double, VD>(store_.deviceView().data(), store_.capacity(), store_.samples()); }
+    PlaneView compensation() {
+        return detail::plane_view<double, VD>(store_.deviceView().data() + VD * store_.capacity(), store_.capacity(),
+                                              store_.samples());
     }
     std::size_t samples() const { return store_.samples(); }
 
@@ -36,10 +38,11 @@ public:
         return *this;
     }
     /** out = value + compensation. */
-    void deliver(const View<double, VD>& out, Stream s = nullptr) { assign(out, value() + compensation(), "set", s); }
+    template <class V>
+    void deliver(const V& out, Stream s = nullptr) { assign(out, Expr(value() + compensation()), "set", s); }
     void zero(Stream s = nullptr) {
-        assign(value(), constant(0.0, View<double, VD>::shape()), "set", s);
-        assign(compensation(), constant(0.0, View<double, VD>::shape()), "set", s);
+        assign(value(), constant(0.0, ir::Shape{int(VD)}), "set", s);
+        assign(compensation(), constant(0.0, ir::Shape{int(VD)}), "set", s);
     }
 
 private:

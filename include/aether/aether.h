@@ -1,31 +1,46 @@
-// aether/aether.h -- the C++ front end of the GB300 engine (umbrella header).
+// aether/aether.h -- the consumer API of the GB300 engine (umbrella header).
 //
-// The consumer surface of the reference's umbrella (aether/aether.h:176-262)
-// for the fused-assignment path: Array<T, Es...> with host and device views,
-// lazy expressions assigned in one statement, aether::math, aether::random.
-// Host code compiles with any C++17 compiler and links libaether_gb300.so;
-// no CUDA compiler is involved on the consumer side: every assignment becomes
-// one sm_103a kernel generated, compiled and cached by the library.
+// The reference's umbrella (aether/aether.h:176-262) for the fused-expression
+// path, in two uses of one set of types:
 //
-//   #include <aether/aether.h>
-//   aether::Array<double, 3> a(n), b(n), c(n), d(n);
-//   aether::random::Generator g(42);
-//   a.deviceView() = g.substream(0).uniform<double, 3>(-1.0, 1.0);
-//   ...
-//   d.deviceView() = a.deviceView() + b.deviceView() * c.deviceView()
-//                    + aether::cwiseSin(a.deviceView()) * aether::cwiseExp((c.deviceView() * c.deviceView()) * -1.0);
-//   d.download();
+// 1. Per-sample code in a consumer's own kernel (a .cu file compiled by nvcc
+//    with -I include): typed views, SampleIndex, expressions, Items and the
+//    math facade evaluate one sample per thread, the reference's model.
+//
+//      AETHER_KERNEL() void k(aether::VecView<double, 3> a, aether::VecView<double, 3> d) {
+//          const aether::SampleIndex i = aether::SampleIndex::make(threadIdx.x, blockIdx.x, blockDim.x);
+//          if (i.global() >= a.samples()) return;
+//          d[i] = a + aether::cwiseSin(a) * aether::cwiseExp((a * a) * -1.0);
+//      }
+//
+// 2. Whole-view assignment from host code (any C++17 compiler, no CUDA
+//    compiler needed): the same expression assigned to a device view on the
+//    host becomes one sm_103a kernel that the library generates, compiles and
+//    caches (aether/eval.h).
+//
+//      aether::Array<double, 3> a(n), b(n), c(n), d(n);
+//      aether::random::Generator g(42);
+//      a.deviceView() = g.substream(0).uniform<double, 3>(-1.0, 1.0);
+//      d.deviceView() = a.deviceView() + b.deviceView() * c.deviceView();
+//      d.download();
 #pragma once
 
-#include "aether/accum.h"
+#include "aether/macros.h"
+#include "aether/layout.h"
+#include "aether/math.h"
+#include "aether/expression.h"
+#include "aether/nodes.h"
+#include "aether/geometry.h"
+#include "aether/view.h"
+#include "aether/item.h"
+#include "aether/random.h"
 #include "aether/array.h"
+#include "aether/eval.h"
+#include "aether/accum.h"
 #include "aether/batch.h"
 #include "aether/device_flag.h"
-#include "aether/eval.h"
-#include "aether/expr.h"
-#include "aether/math.h"
+#include "aether/launch.h"
 #include "aether/partition.h"
-#include "aether/random.h"
 #include "aether/runtime.h"
 
 namespace aether {

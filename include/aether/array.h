@@ -1,16 +1,22 @@
-// aether/array.h -- SoA arrays and their views.
+// aether/array.h -- owning SoA arrays.
 //
-// Array<T, Es...> (array/Array.h:82-364): n samples of a T-valued tensor of
-// static component extents Es..., stored plane by plane: component c of
-// sample i at c * capacity() + i, capacity() = n rounded up to 32 samples
-// (array/Array.h:288-304). An Array owns a pinned host copy and a device copy
-// (chunk/Chunk.h:111-260), both allocated through the C-ABI; upload() and
-// download() move the whole capacity (array/Array.h:250-268).
+// Array<T, Es...> (array/Array.h:82-364): samples() samples of a T-valued
+// tensor of static extents Es..., stored plane by plane: component c of
+// sample s at c * capacity() + s, capacity() a multiple of 32 samples
+// (kCapacityAlignment, array/Array.h:80 and :288-304). An Array owns a pinned
+// host copy and a device copy (chunk/Chunk.h:111-260), allocated through the
+// C-ABI; upload() and download() move the filled samples of every plane,
+// blocking or stream-ordered (array/Array.h:250-268).
 //
-// hostView() reads and writes the host copy with v(c..., i) (view/View.h:
-// 234-246); deviceView() is an expression leaf over the device copy and the
-// destination of an assignment: `d.deviceView() = a.deviceView() + ...;`
-// evaluates the tree for every sample in one kernel (aether/eval.h).
+//   hostView()/deviceView()     View<T, extents<Es..., dyn>, layout_stride>
+//                               over the filled samples (plane stride =
+//                               capacity); const arrays give ConstViewT;
+//   hostPacked()/devicePacked() compact layout_right views, only when the
+//                               array is exactly full (capacity == samples);
+//   hostSpare()/deviceSpare()   the unfilled tail [samples, capacity);
+//   reserve/resize/push_back/clear/commit  growth with the capacity rule
+//                               kept: reallocation copies every plane's
+//                               filled samples, host and device.
 #pragma once
 
 #include <cstddef>
@@ -20,13 +26,19 @@
 #include <type_traits>
 #include <utility>
 
-#include "aether/expr.h"
+#include "aether/item.h"
 #include "aether_gb300.h"
 
 namespace aether {
 
 /** A raw cudaStream_t; nullptr is the legacy default stream. */
 using Stream = void*;
+
+/** Samples rounded up to the 32-sample capacity quantum. */
+inline constexpr std::size_t kCapacityAlignment = 32;
+inline std::size_t quantized_capacity(std::size_t n) {
+    return (n + kCapacityAlignment - 1) / kCapacityAlignment * kCapacityAlignment;
+}
 
 namespace detail {
 
@@ -47,6 +59,7 @@ class Chunk {
 public:
     Chunk() = default;
     Chunk(int kind, std::size_t bytes, const char* where) : kind_(kind), bytes_(bytes) {
+        if (bytes == 0) return;
         void* h = nullptr;
         void* p = nullptr;
         if (aether_chunk_alloc(kind, 0, bytes, nullptr, &h, &p) != AETHER_OK)
@@ -71,6 +84,7 @@ private:
 };
 
 inline void copy(void* dst, int dst_kind, const void* src, int src_kind, std::size_t bytes, Stream s, const char* op) {
+    if (bytes == 0) return;
     if (aether_copy(dst_kind, 0, dst, src_kind, 0, src, bytes, s) != AETHER_OK)
         throw Error::memory(op, dst_kind == AETHER_MEM_DEVICE ? "device 0" : "host", bytes, last_error());
 }
@@ -79,137 +93,98 @@ inline void sync(Stream s) {
     if (aether_stream_sync(0, s) != AETHER_OK) throw Error("stream_sync failed (" + last_error() + ")");
 }
 
+/** Row-major strides of extents<Es..., dyn> with the sample mode at stride 1
+ *  and planes `pitch` samples apart. */
+template <std::size_t... Es>
+struct PlaneStrides {
+    static constexpr std::size_t rank = sizeof...(Es) + 1;
+    offset_t s[rank];
+    explicit PlaneStrides(std::size_t pitch) : s{} {
+        const std::size_t ext[] = {Es..., 1};
+        std::size_t st = pitch;
+        s[rank - 1] = 1;
+        for (std::size_t k = rank - 1; k-- > 0;) {
+            s[k] = static_cast<offset_t>(st);
+            st *= ext[k];
+        }
+    }
+    AETHER_DEVICEANDHOST() offset_t operator[](std::size_t k) const { return s[k]; }
+};
+
+/** The plane-layout view of `n` samples at `ptr`, planes `pitch` apart. */
+template <class T, std::size_t... Es>
+View<T, extents<Es..., dyn>, layout_stride> plane_view(T* ptr, std::size_t pitch, std::size_t n,
+                                                      Device dev = Device(kDLCUDA, 0)) {
+    using X = extents<Es..., dyn>;
+    return View<T, X, layout_stride>(ptr, typename layout_stride::template mapping<X>(X(n), PlaneStrides<Es...>(pitch)),
+                                     dev);
+}
+
 }  // namespace detail
-
-/** A host view: element access v(c0, ..., i) over the pinned host copy. */
-template <class T, std::size_t... Es>
-class HostView {
-public:
-    HostView(T* data, std::size_t pitch, std::size_t n) : data_(data), pitch_(pitch), n_(n) {}
-    template <class... I>
-    T& operator()(I... idx) const {
-        static_assert(sizeof...(I) == sizeof...(Es) + 1 || (sizeof...(Es) == 0 && sizeof...(I) == 1),
-                      "one index per component extent, then the sample");
-        const std::size_t ix[] = {std::size_t(idx)...};
-        constexpr std::size_t ext[] = {Es..., 1};
-        std::size_t c = 0;
-        for (std::size_t k = 0; k + 1 < sizeof...(I); ++k) c = c * ext[k] + ix[k];
-        return data_[c * pitch_ + ix[sizeof...(I) - 1]];
-    }
-    std::size_t samples() const { return n_; }
-    std::size_t pitch() const { return pitch_; }
-    T* data() const { return data_; }
-
-private:
-    T* data_;
-    std::size_t pitch_, n_;
-};
-
-template <class T, std::size_t... Es>
-class View;
-
-/** A device view: an expression leaf and an assignment destination. */
-template <class T, std::size_t... Es>
-class View {
-public:
-    using element_type = T;
-    static constexpr int comps = int((std::size_t(1) * ... * Es));
-
-    View(T* data, std::size_t pitch, std::size_t n) : data_(data), pitch_(pitch), n_(n) {}
-
-    static ir::Shape shape() { return ir::shape_of(extents<Es...>{}); }
-    T* data() const { return data_; }
-    std::size_t pitch() const { return pitch_; }
-    std::size_t samples() const { return n_; }
-
-    /** The view as an expression leaf (view/View.h:369-377). */
-    Expr expr() const {
-        auto n = std::make_shared<ir::Leaf>();
-        n->ptr = data_;
-        n->pitch = pitch_;
-        n->dtype = detail::dtype_name<T>();
-        n->shape = shape();
-        return Expr(n);
-    }
-    operator Expr() const { return expr(); }
-
-    /** Static component I of a vector view as a rank-0 view (View::component<I>,
-     *  view/View.h:315-332). */
-    template <std::size_t I>
-    View<T> component() const {
-        static_assert(sizeof...(Es) == 1, "component<I> of a vector view");
-        return View<T>(data_ + I * pitch_, pitch_, n_);
-    }
-
-    // Assignment launches one kernel (expr/Assign.h:251-346); defined in aether/eval.h.
-    View& operator=(const Expr& e);
-    View& operator+=(const Expr& e);
-    View& operator-=(const Expr& e);
-    View& operator=(const View& o) { return *this = o.expr(); }
-
-    // member surface forwarded to the expression
-    Expr dot(const Expr& o) const { return expr().dot(o); }
-    Expr squaredNorm() const { return expr().squaredNorm(); }
-    Expr norm() const { return expr().norm(); }
-    Expr cross(const Expr& o) const { return expr().cross(o); }
-    Expr quatRotate(const Expr& v) const { return expr().quatRotate(v); }
-    Expr quatMul(const Expr& o) const { return expr().quatMul(o); }
-    Expr inverse() const { return expr().inverse(); }
-    Expr det() const { return expr().det(); }
-    Expr transpose() const { return expr().transpose(); }
-    Expr unitVector() const { return expr().unitVector(); }
-
-private:
-    T* data_;
-    std::size_t pitch_, n_;
-};
-
-// Arithmetic on views goes through their expressions.
-#define AETHER_GB300_VIEW_OP(OPER)                                                                     \
-    template <class T, std::size_t... Es>                                                              \
-    Expr operator OPER(const View<T, Es...>& a, const Expr& b) { return a.expr() OPER b; }           \
-    template <class T, std::size_t... Es>                                                              \
-    Expr operator OPER(const Expr& a, const View<T, Es...>& b) { return a OPER b.expr(); }           \
-    template <class T, std::size_t... Es, class U, std::size_t... Fs>                                  \
-    Expr operator OPER(const View<T, Es...>& a, const View<U, Fs...>& b) { return a.expr() OPER b.expr(); } \
-    template <class T, std::size_t... Es>                                                              \
-    Expr operator OPER(const View<T, Es...>& a, double s) { return a.expr() OPER s; }                 \
-    template <class T, std::size_t... Es>                                                              \
-    Expr operator OPER(double s, const View<T, Es...>& a) { return s OPER a.expr(); }
-AETHER_GB300_VIEW_OP(+)
-AETHER_GB300_VIEW_OP(-)
-AETHER_GB300_VIEW_OP(*)
-#undef AETHER_GB300_VIEW_OP
-template <class T, std::size_t... Es>
-Expr operator/(const View<T, Es...>& a, double s) { return a.expr() / s; }
-template <class T, std::size_t... Es>
-Expr operator-(const View<T, Es...>& a) { return -a.expr(); }
-
-/** Samples rounded up to the 32-sample capacity quantum. */
-inline std::size_t quantized_capacity(std::size_t n) { return (n + 31) / 32 * 32; }
 
 template <class T, std::size_t... Es>
 class Array {
 public:
     using element_type = T;
-    using ViewT = View<T, Es...>;
-    using HostViewT = HostView<T, Es...>;
-    static constexpr std::size_t components = (std::size_t(1) * ... * Es);
+    using Extents = extents<Es..., dyn>;
+    using ViewT = View<T, Extents, layout_stride>;
+    using ConstViewT = View<const T, Extents, layout_stride>;
+    using PackedViewT = View<T, Extents, layout_right>;
+    using ConstPackedViewT = View<const T, Extents, layout_right>;
+    using ItemT = Item<T, Es...>;
+    static constexpr std::size_t components = (Es * ... * std::size_t{1});
 
     explicit Array(std::size_t n_samples)
         : n_(n_samples), cap_(quantized_capacity(n_samples)),
-          host_(AETHER_MEM_PINNED, bytes_(), "host (pinned)"),
-          dev_(AETHER_MEM_DEVICE, bytes_(), "device 0") {}
+          host_(AETHER_MEM_PINNED, bytes_(cap_), "host (pinned)"), dev_(AETHER_MEM_DEVICE, bytes_(cap_), "device 0") {
+        check_span_(cap_);
+    }
 
     std::size_t samples() const { return n_; }
+    std::size_t size() const { return components * n_; }
     std::size_t capacity() const { return cap_; }
-    std::size_t bytes() const { return bytes_(); }
+    std::size_t bytes() const { return bytes_(cap_); }
 
-    HostViewT hostView() { return HostViewT(static_cast<T*>(host_.get()), cap_, n_); }
-    ViewT deviceView() { return ViewT(static_cast<T*>(dev_.get()), cap_, n_); }
+    /** Room for at least n samples (capacity rounded up to 32). */
+    void reserve(std::size_t n) {
+        if (n <= cap_) return;
+        reallocate_(quantized_capacity(n));
+    }
+    void resize(std::size_t n) {
+        if (n > cap_) reserve(n);
+        n_ = n;
+    }
+    /** Append one sample on the host (upload() to publish it). */
+    void push_back(const ItemT& item) {
+        if (n_ == cap_) reserve(cap_ == 0 ? kCapacityAlignment : cap_ * 2);
+        T* base = static_cast<T*>(host_.get());
+        for (std::size_t c = 0; c < components; ++c) base[c * cap_ + n_] = item.data()[c];
+        ++n_;
+    }
+    void clear() { n_ = 0; }
+    /** Mark `count` samples written into the spare tail as filled. */
+    void commit(std::size_t count) {
+        if (count > cap_ - n_)
+            throw Error::memory("Array::commit", "host", bytes_(count),
+                                "count=" + std::to_string(count) + " exceeds spare capacity (" +
+                                    std::to_string(cap_ - n_) + " = capacity()=" + std::to_string(cap_) +
+                                    " - samples()=" + std::to_string(n_) + ")");
+        n_ += count;
+    }
+
+    ViewT hostView() { return strided_<T>(host_, 0, n_, kDLCUDAHost); }
+    ConstViewT hostView() const { return strided_<const T>(host_, 0, n_, kDLCUDAHost); }
+    ViewT deviceView() { return strided_<T>(dev_, 0, n_, kDLCUDA); }
+    ConstViewT deviceView() const { return strided_<const T>(dev_, 0, n_, kDLCUDA); }
+    ViewT hostSpare() { return strided_<T>(host_, n_, cap_ - n_, kDLCUDAHost); }
+    ViewT deviceSpare() { return strided_<T>(dev_, n_, cap_ - n_, kDLCUDA); }
+    PackedViewT hostPacked() { return packed_<T>(host_, kDLCUDAHost); }
+    ConstPackedViewT hostPacked() const { return packed_<const T>(host_, kDLCUDAHost); }
+    PackedViewT devicePacked() { return packed_<T>(dev_, kDLCUDA); }
+    ConstPackedViewT devicePacked() const { return packed_<const T>(dev_, kDLCUDA); }
     ViewT view() { return deviceView(); }
 
-    /** Blocking host -> device copy of the whole capacity. */
+    /** Blocking host -> device copy of every plane. */
     void upload() {
         upload(nullptr);
         detail::sync(nullptr);
@@ -219,23 +194,56 @@ public:
         detail::sync(nullptr);
     }
     /** Stream-ordered copies (array/Array.h:266-268). */
-    void upload(Stream s) { detail::copy(dev_.get(), AETHER_MEM_DEVICE, host_.get(), AETHER_MEM_PINNED, bytes_(), s, "upload"); }
-    void download(Stream s) { detail::copy(host_.get(), AETHER_MEM_PINNED, dev_.get(), AETHER_MEM_DEVICE, bytes_(), s, "download"); }
+    void upload(Stream s) {
+        detail::copy(dev_.get(), AETHER_MEM_DEVICE, host_.get(), AETHER_MEM_PINNED, bytes_(cap_), s, "upload");
+    }
+    void download(Stream s) {
+        detail::copy(host_.get(), AETHER_MEM_PINNED, dev_.get(), AETHER_MEM_DEVICE, bytes_(cap_), s, "download");
+    }
 
 private:
-    std::size_t bytes_() const { return components * cap_ * sizeof(T); }
+    static std::size_t bytes_(std::size_t n) { return components * n * sizeof(T); }
+    static void check_span_(std::size_t cap) {
+        if (components * cap > 0xFFFFFFFFull)
+            throw Error::memory("Array", "device 0", bytes_(cap),
+                                "span exceeds the 32-bit element offsets of device views");
+    }
+    template <class U>
+    View<U, Extents, layout_stride> strided_(const detail::Chunk& c, std::size_t start, std::size_t count,
+                                             int dev) const {
+        using Map = typename layout_stride::template mapping<Extents>;
+        const detail::PlaneStrides<Es...> st(cap_);
+        return View<U, Extents, layout_stride>(static_cast<U*>(c.get()) + start, Map(Extents(count), st),
+                                               Device(dev, 0));
+    }
+    template <class U>
+    View<U, Extents, layout_right> packed_(const detail::Chunk& c, int dev) const {
+        if (cap_ != n_)
+            throw Error::memory("Array::packed", "n/a", bytes_(n_),
+                                "capacity()=" + std::to_string(cap_) + " != samples()=" + std::to_string(n_) +
+                                    ": packed() requires an exactly-full Array (no reserved headroom)");
+        using Map = typename layout_right::template mapping<Extents>;
+        return View<U, Extents, layout_right>(static_cast<U*>(c.get()), Map(Extents(n_)), Device(dev, 0));
+    }
+    void reallocate_(std::size_t cap) {
+        check_span_(cap);
+        detail::Chunk h(AETHER_MEM_PINNED, bytes_(cap), "host (pinned)");
+        detail::Chunk d(AETHER_MEM_DEVICE, bytes_(cap), "device 0");
+        for (std::size_t c = 0; c < components; ++c) {
+            const std::size_t rb = n_ * sizeof(T);
+            detail::copy(static_cast<T*>(h.get()) + c * cap, AETHER_MEM_PINNED, static_cast<T*>(host_.get()) + c * cap_,
+                         AETHER_MEM_PINNED, rb, nullptr, "Array::reserve");
+            detail::copy(static_cast<T*>(d.get()) + c * cap, AETHER_MEM_DEVICE, static_cast<T*>(dev_.get()) + c * cap_,
+                         AETHER_MEM_DEVICE, rb, nullptr, "Array::reserve");
+        }
+        detail::sync(nullptr);
+        host_ = std::move(h);
+        dev_ = std::move(d);
+        cap_ = cap;
+    }
+
     std::size_t n_, cap_;
     detail::Chunk host_, dev_;
 };
-
-/** Batched views by shape (aether.h:234-260). */
-template <class T>
-using ScalarView = View<T>;
-template <class T, std::size_t N>
-using VecView = View<T, N>;
-template <class T, std::size_t R, std::size_t C>
-using MatView = View<T, R, C>;
-using Vec3dView = VecView<double, 3>;
-using Mat33dView = MatView<double, 3, 3>;
 
 }  // namespace aether

@@ -42,10 +42,11 @@ public:
     }
 
     /** dst = e, joined to the batch (evaluated at launch()). */
-    template <class T, std::size_t... Es>
-    void add(const View<T, Es...>& dst, const Expr& e) {
+    template <class V>
+    void add(const V& dst, const Expr& e) {
+        using T = typename V::value_type;
         if (handle_) throw Error("aether Batch: add after the first launch");
-        const ir::Shape shape = dst_shape(View<T, Es...>::shape(), e);
+        const ir::Shape shape = dst_shape(ir::shape_of(typename V::element_extents{}), e);
         Expr ee = e;
         if (e.shape() != shape) {
             if (!e.shape().empty()) throw Error("aether Batch: expression shape does not match the view");
@@ -56,8 +57,8 @@ public:
         it.text = plan_text(dtype, shape, "set", ee, it.ctx);
         it.plan = gb300::detail::plan_for(it.text, dtype, low_);
         it.n = dst.samples();
-        it.dst = dst.data();
-        it.pitch = dst.pitch();
+        it.dst = const_cast<T*>(dst.data());
+        it.pitch = aether::detail::plane_pitch(dst);
         items_.push_back(std::move(it));
     }
 

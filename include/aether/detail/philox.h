@@ -23,7 +23,7 @@ struct Words4 {
     std::uint32_t x, y, z, w;
 };
 
-AETHER_DEVICEHOST() constexpr std::uint64_t splitmix64(std::uint64_t x) {
+AETHER_DEVICEANDHOST() constexpr std::uint64_t splitmix64(std::uint64_t x) {
     x += 0x9E3779B97F4A7C15ull;
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
@@ -31,7 +31,7 @@ AETHER_DEVICEHOST() constexpr std::uint64_t splitmix64(std::uint64_t x) {
 }
 
 /** Ten rounds on counter c under key (kx, ky). */
-AETHER_DEVICEHOST() inline Words4 philox4x32_10(Words4 c, std::uint32_t kx, std::uint32_t ky) {
+AETHER_DEVICEANDHOST() inline Words4 philox4x32_10(Words4 c, std::uint32_t kx, std::uint32_t ky) {
     AETHER_UNROLL
     for (int r = 0; r < 10; ++r) {
         if (r) {
@@ -47,20 +47,20 @@ AETHER_DEVICEHOST() inline Words4 philox4x32_10(Words4 c, std::uint32_t kx, std:
 }
 
 /** The block owned by (key, global sample, counter) (Backend.h:136-150). */
-AETHER_DEVICEHOST() inline Words4 philoxBlock(std::uint64_t key, std::uint32_t global, std::uint64_t counter) {
+AETHER_DEVICEANDHOST() inline Words4 philoxBlock(std::uint64_t key, std::uint32_t global, std::uint64_t counter) {
     return philox4x32_10(Words4{std::uint32_t(counter), std::uint32_t(counter >> 32), global, 0u},
                          std::uint32_t(key), std::uint32_t(key >> 32));
 }
 
 /** (0, 1): w 2^-32 + 2^-33 (double) and (2 (w >> 9) + 1) 2^-24 (float). */
-AETHER_DEVICEHOST() inline double uniformDoubleFromWord(std::uint32_t w) {
+AETHER_DEVICEANDHOST() inline double uniformDoubleFromWord(std::uint32_t w) {
     return double(w) * 2.3283064365386963e-10 + 1.1641532182693481e-10;
 }
-AETHER_DEVICEHOST() inline float uniformFloatFromWord(std::uint32_t w) {
+AETHER_DEVICEANDHOST() inline float uniformFloatFromWord(std::uint32_t w) {
     return float(((w >> 9) << 1) | 1u) * 5.9604645e-8f;
 }
 /** 53-bit uniform from two words: z 2^-53 + 2^-54, z = x ^ (y << 21). */
-AETHER_DEVICEHOST() inline double uniformDoubleHq(std::uint32_t x, std::uint32_t y) {
+AETHER_DEVICEANDHOST() inline double uniformDoubleHq(std::uint32_t x, std::uint32_t y) {
     const std::uint64_t z = std::uint64_t(x) ^ (std::uint64_t(y) << 21);
     return double(z) * 1.1102230246251565e-16 + 5.5511151231257827e-17;
 }

@@ -18,6 +18,7 @@
 #include "aether/array.h"
 #include "aether/expr.h"
 #include "aether_gb300.h"
+#include <cstdint>
 
 namespace aether {
 namespace gb300 {
@@ -98,12 +99,52 @@ inline ir::Shape dst_shape(const ir::Shape& view_shape, const Expr& e) {
     return view_shape;
 }
 
+namespace detail {
+
+/** The plane pitch of a view whose components are planes `pitch` elements
+ *  apart with samples contiguous (every Array view, every layout_right view):
+ *  the only layout the engine's kernels address. Other layouts throw. */
+template <class V>
+std::uint64_t plane_pitch(const V& v) {
+    using X = typename V::extents_type;
+    constexpr std::size_t R = X::Rank;
+    const auto& m = v.mapping();
+    if (m.stride(R - 1) != 1)
+        throw Error("aether assign: the engine's kernels need contiguous samples (sample stride " +
+                    std::to_string(m.stride(R - 1)) + ")");
+    if (R == 1) return v.samples();
+    const std::uint64_t pitch = m.stride(R - 2);
+    std::uint64_t want = pitch;
+    for (std::size_t k = R - 1; k-- > 0;) {
+        if (m.stride(k) != want)
+            throw Error("aether assign: components must be planes of one pitch in row-major order");
+        want *= X::static_extent(k);
+    }
+    if (pitch < v.samples()) throw Error("aether assign: plane pitch smaller than the sample count");
+    return pitch;
+}
+
+}  // namespace detail
+
+/** The IR leaf of a device view (operand slot by pointer and pitch). */
+template <class V>
+Expr gb300_view_leaf(const V& v) {
+    using T = typename V::value_type;
+    auto n = std::make_shared<ir::Leaf>();
+    n->ptr = const_cast<const T*>(v.data());
+    n->pitch = detail::plane_pitch(v);
+    n->dtype = aether::detail::dtype_name<T>();
+    n->shape = ir::shape_of(typename V::element_extents{});
+    return Expr(n);
+}
+
 /** dst <op>= e for every sample of dst, as one kernel on `s`. op: "set",
  *  "add" or "sub". A rank-0 expression broadcasts over dst's components. */
-template <class T, std::size_t... Es>
-void assign(const View<T, Es...>& dst, const Expr& e, const char* op = "set", Stream s = nullptr,
+template <class V>
+void assign(const V& dst, const Expr& e, const char* op = "set", Stream s = nullptr,
             const gb300::Lowering& low = gb300::default_lowering()) {
-    const ir::Shape shape = dst_shape(View<T, Es...>::shape(), e);
+    using T = typename V::value_type;
+    const ir::Shape shape = dst_shape(ir::shape_of(typename V::element_extents{}), e);
     Expr ee = e;
     if (e.shape() != shape) {
         if (!e.shape().empty())
@@ -116,29 +157,18 @@ void assign(const View<T, Es...>& dst, const Expr& e, const char* op = "set", St
     const std::string dtype = aether::detail::dtype_name<T>();
     const std::string text = plan_text(dtype, shape, op, ee, ctx);
     void* plan = gb300::detail::plan_for(text, dtype, low);
-    gb300::detail::launch(plan, ctx, dst.samples(), dst.data(), dst.pitch(), nullptr, s);
+    gb300::detail::launch(plan, ctx, dst.samples(), const_cast<T*>(dst.data()), detail::plane_pitch(dst), nullptr, s);
+}
+
+template <class V, class E>
+void gb300_assign_view(const V& dst, const E& e, const char* op) {
+    assign(dst, Expr(e), op);
 }
 
 /** Alias of assign (the reference's whole-view evaluation, backend/cpu/Tiled.h:185). */
-template <class T, std::size_t... Es>
-void packetEval(const View<T, Es...>& dst, const Expr& e, Stream s = nullptr) {
+template <class V>
+void packetEval(const V& dst, const Expr& e, Stream s = nullptr) {
     assign(dst, e, "set", s);
-}
-
-template <class T, std::size_t... Es>
-View<T, Es...>& View<T, Es...>::operator=(const Expr& e) {
-    assign(*this, e, "set");
-    return *this;
-}
-template <class T, std::size_t... Es>
-View<T, Es...>& View<T, Es...>::operator+=(const Expr& e) {
-    assign(*this, e, "add");
-    return *this;
-}
-template <class T, std::size_t... Es>
-View<T, Es...>& View<T, Es...>::operator-=(const Expr& e) {
-    assign(*this, e, "sub");
-    return *this;
 }
 
 /** Compensated sum over n samples of a rank-0 expression, reduced in a fixed

@@ -1,14 +1,16 @@
-// aether/expr.h -- lazy expressions over SoA arrays, serialised to aether-ir/1.
+// aether/expr.h -- the engine's type-erased expressions (aether-ir/1).
 //
-// The consumer surface of the reference's expression layer: the operators of
+// Expr is a handle on an immutable expression tree whose shape is known at
+// run time: the form every typed expression (aether/expression.h) is
+// serialised to before the engine compiles it, and a builder in its own right
+// for trees assembled at run time. It carries the operators of
 // expr/Operations.h:25-71 (+, -, Hadamard *, s*e, e*s, e/s = e*(1/s)), the
-// elementwise functions of expr/nodes/Elementwise.h:61-854, the member
-// functions of expr/Expression.h:127-486 (dot, squaredNorm, cross,
-// quatRotate, inverse, det, ...) and constant<extents<...>>(v) of
-// expr/nodes/Constant.h:98-150. Building an expression does no work; an
-// assignment (aether/eval.h) serialises the tree to one aether-ir/1 text and
-// runs it as one kernel. Shapes are checked when the tree is built and a
-// mismatch throws aether::Error.
+// elementwise functions of expr/nodes/Elementwise.h:61-854 and the member
+// functions of expr/Expression.h:127-486, with one difference from the typed
+// layer: dot, squaredNorm, norm, sum, det and trace are per-sample folds
+// here. Shapes are checked when the tree is built and a mismatch throws
+// aether::Error. An assignment (aether/eval.h) serialises the tree to one
+// aether-ir/1 text and runs it as one kernel.
 //
 // The text is the same one the Python front end (aether_gb300/expr.py) writes
 // for the same tree, so a plan compiled from either is shared.
@@ -25,6 +27,9 @@
 #include <utility>
 #include <vector>
 
+#include "aether/expression.h"
+#include "aether/layout.h"
+
 namespace aether {
 
 /** Errors of the host API (err/Error.h:30-87): "<op> failed on <where>,
@@ -37,13 +42,6 @@ public:
         return Error(op + " failed on " + where + ", size=" + std::to_string(bytes) + " bytes (" + detail + ")");
     }
 };
-
-/** The trailing dynamic (sample) extent of the reference's extents<...>. */
-inline constexpr std::size_t dyn = static_cast<std::size_t>(-1);
-/** Static component extents (layout/Extents.h:30-146); a trailing `dyn`,
- *  the sample mode, may be spelled or left out. */
-template <std::size_t... Es>
-struct extents {};
 
 namespace ir {
 
@@ -224,6 +222,10 @@ class Expr {
 public:
     Expr() = default;
     explicit Expr(ir::NodeP n) : node_(std::move(n)) {}
+    /** The tree of a typed expression (its type signature, with the operand
+     *  pointers, scalars and keys it holds). */
+    template <class E, std::enable_if_t<aether_expression<E>, int> = 0>
+    Expr(const E& e) : Expr(e.gb300_ir()) {}
     const ir::Shape& shape() const { return node_->shape; }
     bool is_bool() const { return node_->is_bool; }
     const ir::NodeP& node() const { return node_; }
@@ -309,7 +311,7 @@ inline Expr as_expr(const Expr& e, const ir::Shape& shape) {
     if (e.shape().empty() && !shape.empty()) return Expr(ir::bcast(e.node(), shape));
     return e;
 }
-inline void same_shape(const Expr& a, const Expr& b, const char* op) {
+inline void check_same_shape(const Expr& a, const Expr& b, const char* op) {
     if (a.shape() != b.shape())
         throw Error(std::string("aether expression: ") + op + " of shapes " + ir::shape_text(a.shape()) + " and " +
                     ir::shape_text(b.shape()));
@@ -320,7 +322,7 @@ inline void same_shape(const Expr& a, const Expr& b, const char* op) {
 inline Expr operator+(const Expr& a, const Expr& b) {
     const Expr r = detail::as_expr(b, a.shape());
     const Expr l = detail::as_expr(a, r.shape());
-    detail::same_shape(l, r, "+");
+    detail::check_same_shape(l, r, "+");
     return Expr(ir::op("add", {l.node(), r.node()}, l.shape()));
 }
 inline Expr operator+(const Expr& a, double s) { return Expr(ir::op("add", {a.node(), detail::as_expr(s, a.shape()).node()}, a.shape())); }
@@ -328,7 +330,7 @@ inline Expr operator+(double s, const Expr& a) { return Expr(ir::op("add", {deta
 inline Expr operator-(const Expr& a, const Expr& b) {
     const Expr r = detail::as_expr(b, a.shape());
     const Expr l = detail::as_expr(a, r.shape());
-    detail::same_shape(l, r, "-");
+    detail::check_same_shape(l, r, "-");
     return Expr(ir::op("sub", {l.node(), r.node()}, l.shape()));
 }
 inline Expr operator-(const Expr& a, double s) { return Expr(ir::op("sub", {a.node(), detail::as_expr(s, a.shape()).node()}, a.shape())); }
@@ -337,7 +339,7 @@ inline Expr operator-(double s, const Expr& a) { return Expr(ir::op("sub", {deta
 inline Expr operator*(const Expr& a, const Expr& b) {
     if (b.shape().empty() && !a.shape().empty()) return Expr(ir::op("scale", {a.node(), b.node()}, a.shape()));
     if (a.shape().empty() && !b.shape().empty()) return Expr(ir::op("mul", {a.node(), b.node()}, a.shape()));
-    detail::same_shape(a, b, "*");
+    detail::check_same_shape(a, b, "*");
     return Expr(ir::op("mul", {a.node(), b.node()}, a.shape()));
 }
 inline Expr operator*(const Expr& a, double s) { return Expr(ir::op("scale", {a.node(), ir::scalar(s)}, a.shape())); }
@@ -426,10 +428,6 @@ inline ir::NodeP constant_node(double v) {
         return n;
     }
     return ir::scalar(v);
-}
-template <class Extents>
-Expr constant(double v) {
-    return Expr(ir::bcast(constant_node(v), ir::shape_of(Extents{})));
 }
 inline Expr constant(double v, const ir::Shape& shape) { return Expr(ir::bcast(constant_node(v), shape)); }
 /** A scalar baked into the kernel text (compiled once per value). */

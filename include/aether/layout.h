@@ -33,10 +33,10 @@ enum DeviceType : int { kDLCPU = 1, kDLCUDA = 2, kDLCUDAHost = 3 };
 struct Device {
     int type = kDLCPU;
     int id = 0;
-    AETHER_DEVICEHOST() constexpr Device() = default;
-    AETHER_DEVICEHOST() constexpr explicit Device(int t, int i = 0) : type(t), id(i) {}
-    AETHER_DEVICEHOST() constexpr bool operator==(const Device& o) const { return type == o.type && id == o.id; }
-    AETHER_DEVICEHOST() constexpr bool operator!=(const Device& o) const { return !(*this == o); }
+    constexpr Device() = default;
+    AETHER_DEVICEANDHOST() constexpr explicit Device(int t, int i = 0) : type(t), id(i) {}
+    AETHER_DEVICEANDHOST() constexpr bool operator==(const Device& o) const { return type == o.type && id == o.id; }
+    AETHER_DEVICEANDHOST() constexpr bool operator!=(const Device& o) const { return !(*this == o); }
 };
 
 namespace detail {
@@ -46,7 +46,7 @@ struct count_dyn : std::integral_constant<std::size_t, ((Es == dyn ? 1 : 0) + ..
 
 // Compile-time pick of the k-th value of a pack (no array in device memory).
 template <std::size_t... Es>
-AETHER_DEVICEHOST() constexpr std::size_t pick(std::size_t k) {
+AETHER_DEVICEANDHOST() constexpr std::size_t pick(std::size_t k) {
     std::size_t r = 0, j = 0;
     ((r = (j++ == k ? Es : r)), ...);
     return r;
@@ -54,7 +54,7 @@ AETHER_DEVICEHOST() constexpr std::size_t pick(std::size_t k) {
 
 // Position among the dynamic extents of extent k.
 template <std::size_t... Es>
-AETHER_DEVICEHOST() constexpr std::size_t dyn_slot(std::size_t k) {
+AETHER_DEVICEANDHOST() constexpr std::size_t dyn_slot(std::size_t k) {
     std::size_t slot = 0, j = 0;
     ((slot += (j++ < k && Es == dyn) ? 1 : 0), ...);
     return slot;
@@ -69,20 +69,20 @@ public:
     static constexpr std::size_t Rank = sizeof...(Es);
     static constexpr std::size_t RankDynamic = detail::count_dyn<Es...>::value;
 
-    AETHER_DEVICEHOST() static constexpr std::size_t rank() { return Rank; }
-    AETHER_DEVICEHOST() static constexpr std::size_t rank_dynamic() { return RankDynamic; }
+    AETHER_DEVICEANDHOST() static constexpr std::size_t rank() { return Rank; }
+    AETHER_DEVICEANDHOST() static constexpr std::size_t rank_dynamic() { return RankDynamic; }
     /** Extent k as spelled (dyn for a dynamic one). */
-    AETHER_DEVICEHOST() static constexpr std::size_t static_extent(std::size_t k) { return detail::pick<Es...>(k); }
+    AETHER_DEVICEANDHOST() static constexpr std::size_t static_extent(std::size_t k) { return detail::pick<Es...>(k); }
 
-    AETHER_DEVICEHOST() constexpr extents() : dyn_{} {}
+    AETHER_DEVICEANDHOST() constexpr extents() : dyn_{} {}
     template <class... D, class = std::enable_if_t<sizeof...(D) == RankDynamic && (RankDynamic > 0) &&
                                                    (std::is_convertible<D, std::size_t>::value && ...)>>
-    AETHER_DEVICEHOST() constexpr explicit extents(D... d) : dyn_{static_cast<std::size_t>(d)...} {}
+    AETHER_DEVICEANDHOST() constexpr explicit extents(D... d) : dyn_{static_cast<std::size_t>(d)...} {}
 
-    AETHER_DEVICEHOST() constexpr std::size_t extentWide(std::size_t k) const {
+    AETHER_DEVICEANDHOST() constexpr std::size_t extentWide(std::size_t k) const {
         return static_extent(k) == dyn ? dyn_[detail::dyn_slot<Es...>(k)] : static_extent(k);
     }
-    AETHER_DEVICEHOST() constexpr offset_t extent(std::size_t k) const { return static_cast<offset_t>(extentWide(k)); }
+    AETHER_DEVICEANDHOST() constexpr offset_t extent(std::size_t k) const { return static_cast<offset_t>(extentWide(k)); }
 
 private:
     std::size_t dyn_[RankDynamic ? RankDynamic : 1];
@@ -109,23 +109,23 @@ struct layout_right {
     class mapping {
     public:
         using extents_type = Ext;
-        AETHER_DEVICEHOST() constexpr mapping() = default;
-        AETHER_DEVICEHOST() constexpr explicit mapping(const Ext& e) : ext_(e) {}
-        AETHER_DEVICEHOST() constexpr const Ext& extents() const { return ext_; }
-        AETHER_DEVICEHOST() constexpr offset_t stride(std::size_t k) const {
+        constexpr mapping() = default;
+        AETHER_DEVICEANDHOST() constexpr explicit mapping(const Ext& e) : ext_(e) {}
+        AETHER_DEVICEANDHOST() constexpr const Ext& extents() const { return ext_; }
+        AETHER_DEVICEANDHOST() constexpr offset_t stride(std::size_t k) const {
             offset_t s = 1;
             for (std::size_t j = k + 1; j < Ext::Rank; ++j) s *= ext_.extent(j);
             return s;
         }
         template <class... I>
-        AETHER_DEVICEHOST() constexpr offset_t operator()(I... idx) const {
+        AETHER_DEVICEANDHOST() constexpr offset_t operator()(I... idx) const {
             static_assert(sizeof...(I) == Ext::Rank, "one index per extent");
             offset_t off = 0;
             std::size_t k = 0;
             ((off = off * ext_.extent(k++) + static_cast<offset_t>(idx)), ...);
             return off;
         }
-        AETHER_DEVICEHOST() constexpr std::size_t required_span_size() const {
+        AETHER_DEVICEANDHOST() constexpr std::size_t required_span_size() const {
             std::size_t s = 1;
             for (std::size_t k = 0; k < Ext::Rank; ++k) s *= ext_.extentWide(k);
             return s;
@@ -144,27 +144,27 @@ struct layout_stride {
     class mapping {
     public:
         using extents_type = Ext;
-        AETHER_DEVICEHOST() constexpr mapping() : ext_(), s_{} {}
+        AETHER_DEVICEANDHOST() constexpr mapping() : ext_(), s_{} {}
         template <class S>
-        AETHER_DEVICEHOST() constexpr mapping(const Ext& e, const S& strides) : ext_(e), s_{} {
+        AETHER_DEVICEANDHOST() constexpr mapping(const Ext& e, const S& strides) : ext_(e), s_{} {
             for (std::size_t k = 0; k < Ext::Rank; ++k) s_[k] = static_cast<offset_t>(strides[k]);
         }
         /** From another mapping of the same extents (e.g. layout_right's). */
         template <class M, class = decltype(std::declval<const M&>().stride(0))>
-        AETHER_DEVICEHOST() constexpr explicit mapping(const M& m) : ext_(m.extents()), s_{} {
+        AETHER_DEVICEANDHOST() constexpr explicit mapping(const M& m) : ext_(m.extents()), s_{} {
             for (std::size_t k = 0; k < Ext::Rank; ++k) s_[k] = m.stride(k);
         }
-        AETHER_DEVICEHOST() constexpr const Ext& extents() const { return ext_; }
-        AETHER_DEVICEHOST() constexpr offset_t stride(std::size_t k) const { return s_[k]; }
+        AETHER_DEVICEANDHOST() constexpr const Ext& extents() const { return ext_; }
+        AETHER_DEVICEANDHOST() constexpr offset_t stride(std::size_t k) const { return s_[k]; }
         template <class... I>
-        AETHER_DEVICEHOST() constexpr offset_t operator()(I... idx) const {
+        AETHER_DEVICEANDHOST() constexpr offset_t operator()(I... idx) const {
             static_assert(sizeof...(I) == Ext::Rank, "one index per extent");
             offset_t off = 0;
             std::size_t k = 0;
             ((off += static_cast<offset_t>(idx) * s_[k++]), ...);
             return off;
         }
-        AETHER_DEVICEHOST() constexpr std::size_t required_span_size() const {
+        AETHER_DEVICEANDHOST() constexpr std::size_t required_span_size() const {
             std::size_t s = 1;
             for (std::size_t k = 0; k < Ext::Rank; ++k) {
                 if (ext_.extentWide(k) == 0) return 0;
@@ -183,14 +183,14 @@ struct layout_stride {
  *  (index/SampleIndex.h:46-71): global() is the grid-wide sample,
  *  work() the block-local slot. */
 struct SampleIndex {
-    AETHER_DEVICEHOST() static constexpr SampleIndex make(offset_t threadIdxx, offset_t blockIdxx, offset_t blockDimx) {
+    AETHER_DEVICEANDHOST() static constexpr SampleIndex make(offset_t threadIdxx, offset_t blockIdxx, offset_t blockDimx) {
         return SampleIndex{blockIdxx * blockDimx + threadIdxx, threadIdxx};
     }
-    AETHER_DEVICEHOST() static constexpr SampleIndex make(std::size_t index) {
+    AETHER_DEVICEANDHOST() static constexpr SampleIndex make(std::size_t index) {
         return SampleIndex{static_cast<offset_t>(index), static_cast<offset_t>(index)};
     }
-    AETHER_DEVICEHOST() constexpr offset_t global() const { return globalIdx_; }
-    AETHER_DEVICEHOST() constexpr offset_t work() const { return workIdx_; }
+    AETHER_DEVICEANDHOST() constexpr offset_t global() const { return globalIdx_; }
+    AETHER_DEVICEANDHOST() constexpr offset_t work() const { return workIdx_; }
 
     offset_t globalIdx_;
     offset_t workIdx_;

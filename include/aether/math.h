@@ -1,51 +1,172 @@
-// aether/math.h -- the scalar math facade on the host.
+// aether/math.h -- the scalar math facade, host and device.
 //
 // aether::math (math/math.h:82-287) names one function per operation for
-// per-sample code; on the host the reference routes to std:: (math/detail/
-// MathDispatch.h:54-112), with rsqrt as 1/std::sqrt (math/root.h:63-76) and
-// log1p/expm1 from <cmath> (math/explog.h:38-81). Device code of this engine
-// is generated per expression (the kernels evaluate the elementwise nodes of
-// aether/expr.h), so only the host half is declared here.
+// per-sample code. As in the reference's dispatch (math/detail/
+// MathDispatch.h:54-112) the host routes to std:: and the device to CUDA's
+// functions, with two choices of this engine:
+//   * rsqrt is 1/sqrt(x) with both steps correctly rounded on both sides (the
+//     host spelling of math/root.h:63-76), so a device result equals the
+//     reference's CPU result bit for bit;
+//   * a consumer translation unit compiled with AETHER_GB300_EMULATED_FP64
+//     defined evaluates the double sqrt, rsqrt, exp, log, log1p, sin and cos
+//     in double-float arithmetic on the FP32/INT pipes (aether/gb300/
+//     ag_emu64.cuh, the lowering of the engine's emulated plans): about 2^-46
+//     relative per function instead of 2^-53, far faster on GB300's FP64
+//     pipe. Arguments outside that arithmetic's range (|x| outside [2^-50,
+//     2^60], exp arguments outside (-70, 87), trig arguments beyond 2^24,
+//     special values) and results that would not reassemble exactly take
+//     CUDA's FP64 function instead, so range and special values keep FP64
+//     semantics.
+// Every function is usable from device and host code.
 #pragma once
 
 #include <cmath>
 
+#include "aether/macros.h"
+
+#if defined(__CUDACC__) && defined(AETHER_GB300_EMULATED_FP64)
+#include "aether/gb300/ag_device.cuh"
+#include "aether/gb300/ag_emu64.cuh"
+#endif
+
 namespace aether {
 namespace math {
 
-template <class T> inline T sqrt(T x) { return std::sqrt(x); }
-template <class T> inline T rsqrt(T x) { return T(1) / std::sqrt(x); }
-template <class T> inline T cbrt(T x) { return std::cbrt(x); }
-template <class T> inline T exp(T x) { return std::exp(x); }
-template <class T> inline T exp2(T x) { return std::exp2(x); }
-template <class T> inline T expm1(T x) { return std::expm1(x); }
-template <class T> inline T log(T x) { return std::log(x); }
-template <class T> inline T log2(T x) { return std::log2(x); }
-template <class T> inline T log10(T x) { return std::log10(x); }
-template <class T> inline T log1p(T x) { return std::log1p(x); }
-template <class T> inline T sin(T x) { return std::sin(x); }
-template <class T> inline T cos(T x) { return std::cos(x); }
-template <class T> inline T tan(T x) { return std::tan(x); }
-template <class T> inline T asin(T x) { return std::asin(x); }
-template <class T> inline T acos(T x) { return std::acos(x); }
-template <class T> inline T atan(T x) { return std::atan(x); }
-template <class T> inline T atan2(T y, T x) { return std::atan2(y, x); }
-template <class T> inline T sinh(T x) { return std::sinh(x); }
-template <class T> inline T cosh(T x) { return std::cosh(x); }
-template <class T> inline T tanh(T x) { return std::tanh(x); }
-template <class T> inline T erf(T x) { return std::erf(x); }
-template <class T> inline T abs(T x) { return std::fabs(x); }
-template <class T> inline T floor(T x) { return std::floor(x); }
-template <class T> inline T ceil(T x) { return std::ceil(x); }
-template <class T> inline T trunc(T x) { return std::trunc(x); }
-template <class T> inline T pow(T x, T y) { return std::pow(x, y); }
-template <class T> inline T hypot(T x, T y) { return std::hypot(x, y); }
-template <class T> inline T fma(T a, T b, T c) { return std::fma(a, b, c); }
-template <class T> inline T min(T a, T b) { return std::fmin(a, b); }
-template <class T> inline T max(T a, T b) { return std::fmax(a, b); }
-template <class T> inline void sincos(T x, T* s, T* c) {
-    *s = std::sin(x);
-    *c = std::cos(x);
+#if defined(__CUDA_ARCH__) && defined(AETHER_GB300_EMULATED_FP64)
+namespace emu {
+// One double-float evaluation of f at x, or CUDA's FP64 function where the
+// double-float path cannot answer.
+#define AETHER_GB300_EMU1(NAME, BODY, NATIVE)                                  \
+    __device__ inline double NAME(double x) {                                  \
+        bool ok = true;                                                        \
+        const ::ag::e64::df v = ::ag::e64::from_double_ck(x, ok);              \
+        const ::ag::e64::df r = BODY;                                          \
+        const double y = ::ag::e64::to_double(r);                              \
+        return (ok && ::ag::e64::out_ok(r) && y == y) ? y : NATIVE(x);         \
+    }
+__device__ inline double native_rsqrt(double x) { return __ddiv_rn(1.0, __dsqrt_rn(x)); }
+AETHER_GB300_EMU1(sqrt, ::ag::e64::sqrt_(v), __dsqrt_rn)
+AETHER_GB300_EMU1(rsqrt, ::ag::e64::rsqrt_(v), native_rsqrt)
+AETHER_GB300_EMU1(exp, ::ag::e64::exp_(v, ok), ::exp)
+AETHER_GB300_EMU1(log, ::ag::e64::log_(v), ::log)
+AETHER_GB300_EMU1(log1p, ::ag::e64::log1p_(v), ::log1p)
+AETHER_GB300_EMU1(sin, ::ag::e64::sin_(v, ok), ::sin)
+AETHER_GB300_EMU1(cos, ::ag::e64::cos_(v, ok), ::cos)
+#undef AETHER_GB300_EMU1
+}  // namespace emu
+#define AETHER_GB300_D(EMU, NATIVE) EMU
+#else
+#define AETHER_GB300_D(EMU, NATIVE) NATIVE
+#endif
+
+// -- one-argument functions -------------------------------------------------
+#if defined(__CUDA_ARCH__)
+#define AETHER_MATH1(NAME, DDEV, FDEV, HOST)                                                \
+    AETHER_DEVICEANDHOST() inline double NAME(double x) { return DDEV(x); }                 \
+    AETHER_DEVICEANDHOST() inline float NAME(float x) { return FDEV(x); }
+#else
+#define AETHER_MATH1(NAME, DDEV, FDEV, HOST)                                                \
+    AETHER_DEVICEANDHOST() inline double NAME(double x) { return HOST(x); }                 \
+    AETHER_DEVICEANDHOST() inline float NAME(float x) { return HOST(x); }
+#endif
+
+#if defined(__CUDA_ARCH__)
+namespace dev {
+__device__ inline double rsqrt(double x) { return __ddiv_rn(1.0, __dsqrt_rn(x)); }
+__device__ inline float rsqrt(float x) { return __fdiv_rn(1.0f, __fsqrt_rn(x)); }
+__device__ inline double sqrt(double x) { return __dsqrt_rn(x); }
+__device__ inline float sqrt(float x) { return __fsqrt_rn(x); }
+}  // namespace dev
+#endif
+namespace host {
+template <class T>
+inline T rsqrt(T x) { return T(1) / std::sqrt(x); }
+}  // namespace host
+
+AETHER_MATH1(sqrt, AETHER_GB300_D(emu::sqrt, dev::sqrt), dev::sqrt, std::sqrt)
+AETHER_MATH1(rsqrt, AETHER_GB300_D(emu::rsqrt, dev::rsqrt), dev::rsqrt, host::rsqrt)
+AETHER_MATH1(exp, AETHER_GB300_D(emu::exp, ::exp), ::expf, std::exp)
+AETHER_MATH1(log, AETHER_GB300_D(emu::log, ::log), ::logf, std::log)
+AETHER_MATH1(log1p, AETHER_GB300_D(emu::log1p, ::log1p), ::log1pf, std::log1p)
+AETHER_MATH1(sin, AETHER_GB300_D(emu::sin, ::sin), ::sinf, std::sin)
+AETHER_MATH1(cos, AETHER_GB300_D(emu::cos, ::cos), ::cosf, std::cos)
+AETHER_MATH1(cbrt, ::cbrt, ::cbrtf, std::cbrt)
+AETHER_MATH1(exp2, ::exp2, ::exp2f, std::exp2)
+AETHER_MATH1(expm1, ::expm1, ::expm1f, std::expm1)
+AETHER_MATH1(log2, ::log2, ::log2f, std::log2)
+AETHER_MATH1(log10, ::log10, ::log10f, std::log10)
+AETHER_MATH1(tan, ::tan, ::tanf, std::tan)
+AETHER_MATH1(asin, ::asin, ::asinf, std::asin)
+AETHER_MATH1(acos, ::acos, ::acosf, std::acos)
+AETHER_MATH1(atan, ::atan, ::atanf, std::atan)
+AETHER_MATH1(sinh, ::sinh, ::sinhf, std::sinh)
+AETHER_MATH1(cosh, ::cosh, ::coshf, std::cosh)
+AETHER_MATH1(tanh, ::tanh, ::tanhf, std::tanh)
+AETHER_MATH1(erf, ::erf, ::erff, std::erf)
+AETHER_MATH1(abs, ::fabs, ::fabsf, std::fabs)
+AETHER_MATH1(floor, ::floor, ::floorf, std::floor)
+AETHER_MATH1(ceil, ::ceil, ::ceilf, std::ceil)
+AETHER_MATH1(trunc, ::trunc, ::truncf, std::trunc)
+#undef AETHER_MATH1
+#undef AETHER_GB300_D
+
+// -- two- and three-argument functions ---------------------------------------
+#if defined(__CUDA_ARCH__)
+#define AETHER_MATH2(NAME, DDEV, FDEV, HOST)                                                       \
+    AETHER_DEVICEANDHOST() inline double NAME(double a, double b) { return DDEV(a, b); }          \
+    AETHER_DEVICEANDHOST() inline float NAME(float a, float b) { return FDEV(a, b); }
+#else
+#define AETHER_MATH2(NAME, DDEV, FDEV, HOST)                                                       \
+    AETHER_DEVICEANDHOST() inline double NAME(double a, double b) { return HOST(a, b); }          \
+    AETHER_DEVICEANDHOST() inline float NAME(float a, float b) { return HOST(a, b); }
+#endif
+AETHER_MATH2(pow, ::pow, ::powf, std::pow)
+AETHER_MATH2(atan2, ::atan2, ::atan2f, std::atan2)
+AETHER_MATH2(hypot, ::hypot, ::hypotf, std::hypot)
+AETHER_MATH2(min, ::fmin, ::fminf, std::fmin)
+AETHER_MATH2(max, ::fmax, ::fmaxf, std::fmax)
+#undef AETHER_MATH2
+
+AETHER_DEVICEANDHOST() inline double fma(double a, double b, double c) {
+#if defined(__CUDA_ARCH__)
+    return __fma_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+AETHER_DEVICEANDHOST() inline float fma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+
+template <class T>
+AETHER_DEVICEANDHOST() inline void sincos(T x, T* s, T* c) {
+    *s = math::sin(x);
+    *c = math::cos(x);
+}
+
+AETHER_DEVICEANDHOST() inline bool isfinite(double x) {
+#if defined(__CUDA_ARCH__)
+    return ::isfinite(x);
+#else
+    return std::isfinite(x);
+#endif
+}
+AETHER_DEVICEANDHOST() inline bool isfinite(float x) {
+#if defined(__CUDA_ARCH__)
+    return ::isfinite(x);
+#else
+    return std::isfinite(x);
+#endif
+}
+
+/** -1, 0 or +1 (the sign of math/round.h's sign(), NaN -> 0). */
+template <class T>
+AETHER_DEVICEANDHOST() constexpr T sign(T x) {
+    return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0));
 }
 
 }  // namespace math

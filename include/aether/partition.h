@@ -29,8 +29,9 @@ inline std::size_t padded_block_samples(std::size_t n, std::size_t parts, std::s
     return (per + pad_to - 1) / pad_to * pad_to;
 }
 
-template <class T, std::size_t... Es>
-View<T, Es...> partition_view(const View<T, Es...>& v, const PartitionSpec& spec, std::size_t r) {
+template <class T, class X, class L, bool Vo, bool RO>
+View<T, X, layout_stride, Vo, RO> partition_view(const View<T, X, L, Vo, RO>& v, const PartitionSpec& spec,
+                                                  std::size_t r) {
     if (r >= spec.parts)
         throw Error::memory("partition_view", "cuda:0", 0,
                             "block index " + std::to_string(r) + " >= spec.parts=" + std::to_string(spec.parts));
@@ -38,7 +39,13 @@ View<T, Es...> partition_view(const View<T, Es...>& v, const PartitionSpec& spec
     const std::size_t padded = padded_block_samples(n, spec.parts, spec.pad_to);
     const std::size_t off = r * padded;
     const std::size_t real = off < n ? (padded < n - off ? padded : n - off) : 0;
-    return View<T, Es...>(v.data() + off, v.pitch(), real);
+    // the same strides, the sample extent cut to the block
+    using Map = typename layout_stride::template mapping<X>;
+    offset_t st[X::Rank];
+    for (std::size_t k = 0; k < X::Rank; ++k) st[k] = v.mapping().stride(k);
+    const std::size_t start = off < n ? off : n;
+    return View<T, X, layout_stride, Vo, RO>(const_cast<T*>(v.data()) + start * st[X::Rank - 1],
+                                             Map(X(real), st), v.device());
 }
 
 }  // namespace aether

@@ -17,25 +17,22 @@ namespace aether {
 
 using RuntimeView = AetherRuntimeView;
 
-/** The descriptor of a device view: modes (components..., samples). */
-template <class T, std::size_t... Es>
-RuntimeView fromView(const View<T, Es...>& v) {
+/** The descriptor of a device view: its modes (components..., samples) with
+ *  the view's own element strides (view/RuntimeView.h:71-110). */
+template <class T, class X, class L, bool Vo, bool RO>
+RuntimeView fromView(const View<T, X, L, Vo, RO>& v) {
+    static_assert(X::Rank <= AETHER_RT_RANK_CAP, "runtime views have at most six modes");
+    using U = std::remove_cv_t<T>;
     RuntimeView r{};
-    r.data = v.data();
+    r.data = const_cast<U*>(v.data());
     r.dtype_code = 2;
-    r.dtype_bits = uint8_t(sizeof(T) * 8);
+    r.dtype_bits = uint8_t(sizeof(U) * 8);
     r.dtype_lanes = 1;
-    const std::size_t ext[] = {Es..., 0};
-    const int rank = int(sizeof...(Es)) + 1;
-    r.rank = rank;
-    int64_t stride = int64_t(v.pitch());
-    for (int k = rank - 2; k >= 0; --k) {
-        r.extents[k] = int64_t(ext[k]);
-        r.strides[k] = stride;
-        stride *= int64_t(ext[k]);
+    r.rank = int32_t(X::Rank);
+    for (std::size_t k = 0; k < X::Rank; ++k) {
+        r.extents[k] = int64_t(v.extent(k));
+        r.strides[k] = int64_t(v.mapping().stride(k));
     }
-    r.extents[rank - 1] = int64_t(v.samples());
-    r.strides[rank - 1] = 1;
     return r;
 }
 

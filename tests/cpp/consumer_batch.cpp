@@ -29,9 +29,9 @@ int main() {
         ms.emplace_back(new Array<double, 3, 3>(n));
         minv.emplace_back(new Array<double, 3, 3>(n));
         mref.emplace_back(new Array<double, 3, 3>(n));
-        ms.back()->deviceView() = g.substream(100 + k).uniform<double, 9>(-1.0, 1.0).reshape({3, 3});
+        ms.back()->deviceView() = Expr(g.substream(100 + k).uniform<double, 9>(-1.0, 1.0)).reshape({3, 3});
         auto M = ms.back()->deviceView();
-        const Expr inv = select(cwiseAbs(M.det()) > 1e-300, M.inverse(), constant<extents<3, 3>>(0.0));
+        const Expr inv = select(cwiseAbs(per_sample::det(M)) > 1e-300, M.inverse(), constant<extents<3, 3>>(0.0));
         mref.back()->deviceView() = inv;
         batch.add(minv.back()->deviceView(), inv);
     }
@@ -62,7 +62,8 @@ int main() {
     if (batch.info().n_plans != 2) return 1;
 
     // serving: the cross products again, operands from the arrays' host copies
-    View<double, 3> pa(reinterpret_cast<double*>(16), 0, 0), pb(reinterpret_cast<double*>(32), 0, 0);
+    auto pa = aether::detail::plane_view<double, 3>(reinterpret_cast<double*>(16), 0, 0);
+    auto pb = aether::detail::plane_view<double, 3>(reinterpret_cast<double*>(32), 0, 0);
     gb300::Server srv(64ull << 20);
     const int cross = srv.add_shape({pa, pb}, pa.cross(pb), "f64", {3});
     srv.open();

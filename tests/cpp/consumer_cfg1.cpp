@@ -19,7 +19,7 @@ int main(int argc, char** argv) {
     c.deviceView() = g.substream(2).uniform<double, 3>(-1.0, 1.0);
     auto A = a.deviceView(), B = b.deviceView(), C = c.deviceView();
     d.deviceView() = A + B * C + aether::cwiseSin(A) * aether::cwiseExp((C * C) * -1.0);
-    const auto sum = aether::globalSum(A.dot(B), n);
+    const auto sum = aether::globalSum(aether::per_sample::dot(A, B), n);
     a.download();
     b.download();
     c.download();
@@ -72,7 +72,7 @@ int main(int argc, char** argv) {
                 }
     }
     try {
-        d.deviceView() = A.dot(B) + aether::constant<aether::extents<2>>(1.0);
+        d.deviceView() = aether::Expr(aether::per_sample::dot(A, B)) + aether::Expr(aether::constant<aether::extents<2>>(1.0));
         std::printf("shape mismatch was not refused\n");
         return 1;
     } catch (const aether::Error&) {

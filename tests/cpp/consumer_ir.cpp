@@ -1,7 +1,7 @@
 // Consumer-side check of the C++ front end without a device: builds the
-// expressions of the reference configurations through include/aether and
-// prints the aether-ir/1 text of each assignment, one per line, for the
-// Python test to compare with the Python front end's text.
+// expressions of the reference configurations as typed expressions through
+// include/aether and prints the aether-ir/1 text each serialises to, one per
+// line, for the Python test to compare with the Python front end's text.
 #include <aether/aether.h>
 
 #include <cstdio>
@@ -9,14 +9,16 @@
 using namespace aether;
 
 template <class T, std::size_t... Es>
-View<T, Es...> fake(std::uintptr_t addr, std::size_t n) {
-    return View<T, Es...>(reinterpret_cast<T*>(addr), quantized_capacity(n), n);
+auto fake(std::uintptr_t addr, std::size_t n) {
+    return aether::detail::plane_view<T, Es...>(reinterpret_cast<T*>(addr), quantized_capacity(n), n);
 }
 
-template <class T, std::size_t... Es>
-void emit(const char* name, const View<T, Es...>&, const Expr& e, const char* op = "set") {
+template <class V, class E>
+void emit(const char* name, const V&, const E& typed, const char* op = "set") {
+    const Expr e(typed);
     ir::Context ctx;
-    const std::string text = plan_text(aether::detail::dtype_name<T>(), dst_shape(View<T, Es...>::shape(), e), op, e, ctx);
+    const std::string text = plan_text(aether::detail::dtype_name<typename V::value_type>(),
+                                       dst_shape(ir::shape_of(typename V::element_extents{}), e), op, e, ctx);
     std::printf("%s\t%s\t%zu\t%zu\t%zu\n", name, text.c_str(), ctx.operands.size(), ctx.scalars.size(), ctx.keys.size());
 }
 
@@ -34,13 +36,13 @@ int main() {
     auto m = fake<double, 3, 3>(0x80000, n), mi = fake<double, 3, 3>(0x90000, n);
     emit("cross", d, a.cross(b));
     emit("qrot", d, q.quatRotate(b));
-    emit("inv", mi, select(cwiseAbs(m.det()) > 1e-300, m.inverse(), constant<extents<3, 3>>(0.0)));
+    emit("inv", mi, select(cwiseAbs(per_sample::det(m)) > 1e-300, m.inverse(), constant<extents<3, 3>>(0.0)));
     auto x = fake<float, 8>(0xA0000, n), y = fake<float, 8>(0xB0000, n);
     auto s = fake<float>(0xC0000, n);
-    emit("dot8", s, x.dot(y));
+    emit("dot8", s, per_sample::dot(x, y));
     emit("axpy_add", d, a * 2.5 + b / 4.0, "add");
     emit("minmax", d, cwiseMax(cwiseMin(a, b), -0.5) - clamp(c, -0.25, 0.25));
-    emit("structural", d, m.expr().row(1) + m.expr().col(2) + m.expr().transpose().matvec(a));
+    emit("structural", d, m.row<1>() + m.col<2>() + m.transpose() * a);
     emit("literal", d, a * literal(0.1) + literal(-3.0));
     return 0;
 }

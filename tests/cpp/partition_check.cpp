@@ -37,18 +37,18 @@ int main() {
     CHECK(threw);
 
     static double buf[3 * 100];
-    aether::View<double, 3> full(buf, 100, 100);
+    auto full = aether::detail::plane_view<double, 3>(buf, 100, 100, aether::Device(aether::kDLCPU));
     const aether::PartitionSpec spec{4, 32};
     const std::size_t off[4] = {0, 32, 64, 96}, real[4] = {32, 32, 32, 4};
     for (std::size_t r = 0; r < 4; ++r) {
         auto b = aether::partition_view(full, spec, r);
         CHECK(b.samples() == real[r]);
         CHECK(b.data() == buf + off[r]);
-        CHECK(b.pitch() == 100);
+        CHECK(b.mapping().stride(0) == 100 && b.mapping().stride(1) == 1);
         const auto rt = aether::fromView(b);
         CHECK(rt.extents[0] == 3 && rt.extents[1] == int64_t(real[r]) && rt.strides[0] == 100 && rt.strides[1] == 1);
     }
-    aether::View<double, 3> exact(buf, 96, 96);
+    auto exact = aether::detail::plane_view<double, 3>(buf, 96, 96, aether::Device(aether::kDLCPU));
     for (std::size_t r = 0; r < 3; ++r) {
         auto b = aether::partition_view(exact, aether::PartitionSpec{3, 32}, r);
         CHECK(b.samples() == 32 && b.data() == buf + r * 32);
