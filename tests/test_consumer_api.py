@@ -164,3 +164,18 @@ def test_consumer_kernels_on_device(tmp_path, oracle, variant):
     assert np.array_equal(res["cr"], res["cr2"])
     bound = "native" if variant != "emulated" else acc.EMU_EXPR_BOUND_2M53
     check_results(oracle, res, n, exact_arith=(variant == "exact"), bound_expr=bound)
+
+
+@pytest.mark.gpu
+def test_array_growth_surface(tmp_path):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    cxx = shutil.which("g++") or shutil.which("c++")
+    exe = str(tmp_path / "consumer_array")
+    src = os.path.join(REPO, "tests", "cpp", "consumer_array.cpp")
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-I", INCLUDE, src, "-o", exe, "-L", LIBDIR,
+                        "-laether_gb300", "-Wl,-rpath," + LIBDIR], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0 and "array ok" in run.stdout, run.stdout + run.stderr
