@@ -146,6 +146,9 @@ _SIGS = {
     "aether_rtc_digest": (ctypes.c_uint64, []),
     "aether_plan_cache_key": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
                                              ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "aether_rtc_compile": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p),
+                                          ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_size_t)]),
 }
 
 _lib = None

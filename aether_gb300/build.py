@@ -33,6 +33,11 @@ DEVICE_INC = os.path.join(REPO, "include", "aether", "gb300")
 EMBED = [("kAgDeviceSrc", "ag_device.cuh"), ("kAgEmu64Src", "ag_emu64.cuh"),
          ("kAgEmu64TablesSrc", "ag_emu64_tables.cuh"), ("kAgEmu64BmSrc", "ag_emu64_bm.cuh"),
          ("kAgEmu64BmTablesSrc", "ag_emu64_bm_tables.cuh")]
+# The device-safe consumer headers (aether/device.h and what it includes),
+# exported with the engine's device runtime as the NVRTC payload for code
+# generators, each under its include name.
+CONSUMER_HEADERS = ["macros.h", "detail/std.h", "layout.h", "math.h", "expression.h", "nodes.h", "geometry.h",
+                    "view.h", "item.h", "detail/philox.h", "random.h", "device.h"]
 EXPORT_PREFIX = "aether_"
 
 
@@ -63,6 +68,17 @@ def _embed():
         pieces = [src[i:i + 12000] for i in range(0, len(src), 12000)] or [""]
         body = "\n".join('R"%s(%s)%s"' % (delim, p, delim) for p in pieces)
         parts.append("static const char* const %s =\n%s;\n" % (name, body))
+    table = []
+    for k, rel in enumerate(CONSUMER_HEADERS):
+        src = open(os.path.join(REPO, "include", "aether", rel)).read()
+        delim = "AGSRC"
+        assert ")" + delim + '"' not in src
+        pieces = [src[i:i + 12000] for i in range(0, len(src), 12000)] or [""]
+        body = "\n".join('R"%s(%s)%s"' % (delim, p, delim) for p in pieces)
+        parts.append("static const char* const kConsumer%d =\n%s;\n" % (k, body))
+        table.append('    {"aether/%s", kConsumer%d},\n' % (rel, k))
+    parts.append("struct AgNamedSource {\n    const char* name;\n    const char* src;\n};\n")
+    parts.append("static const AgNamedSource kConsumerHeaders[] = {\n%s};\n" % "".join(table))
     _write_if_changed(os.path.join(BUILD, "embedded.inc"), "".join(parts))
 
 

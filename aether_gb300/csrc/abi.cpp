@@ -789,6 +789,24 @@ AG_EXPORT int aether_plan_cache_key(const char* source, const char* arch, const 
     });
 }
 
+AG_EXPORT int aether_rtc_compile(const char* source, const char* arch, const char* const* options, int n_options,
+                                 void* cubin, size_t cap, size_t* len) {
+    return guarded([&] {
+        if (!source || !arch || !len || (n_options > 0 && !options))
+            throw std::runtime_error("rtc_compile: null argument");
+        std::vector<std::string> opts;
+        for (int i = 0; i < n_options; ++i) opts.push_back(options[i] ? options[i] : "");
+        const std::string bin = ag::compile_with_payload(source, arch, opts);
+        *len = bin.size();
+        if (cubin) {
+            if (cap < bin.size())
+                throw std::runtime_error("rtc_compile: buffer of " + std::to_string(cap) + " bytes, " +
+                                         std::to_string(bin.size()) + " needed");
+            std::memcpy(cubin, bin.data(), bin.size());
+        }
+    });
+}
+
 AG_EXPORT void aether_plan_release(void* plan) {
     PlanObj* P = static_cast<PlanObj*>(plan);
     if (!P) return;

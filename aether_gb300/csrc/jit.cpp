@@ -21,6 +21,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 #include <unordered_map>
+#include <vector>
 
 #include "embedded.inc"   // kAgDeviceSrc, kAgEmu64Src, ... (the device headers as literals)
 
@@ -96,20 +97,49 @@ constexpr int kNumHeaders = int(sizeof(kHeaders) / sizeof(kHeaders[0]));
 
 }  // namespace
 
-int payload_count() { return kNumHeaders; }
+// The NVRTC payload: the engine's device runtime under its bare include names
+// (as generated plans include it), the device-safe consumer headers under
+// "aether/...", and the device runtime again under "aether/gb300/..." (as the
+// consumer headers include it).
+constexpr int kNumConsumer = int(sizeof(kConsumerHeaders) / sizeof(kConsumerHeaders[0]));
+constexpr int kNumPayload = kNumHeaders + kNumConsumer + kNumHeaders;
+
+namespace {
+const std::string& gb300_name(int i) {
+    static std::string names[kNumHeaders];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (int k = 0; k < kNumHeaders; ++k) names[k] = std::string("aether/gb300/") + kHeaders[k].name;
+    });
+    return names[i];
+}
+}  // namespace
+
+int payload_count() { return kNumPayload; }
 
 bool payload_header(int i, const char** name, const char** src) {
-    if (i < 0 || i >= kNumHeaders) return false;
-    *name = kHeaders[i].name;
-    *src = kHeaders[i].src;
+    if (i < 0 || i >= kNumPayload) return false;
+    if (i < kNumHeaders) {
+        *name = kHeaders[i].name;
+        *src = kHeaders[i].src;
+    } else if (i < kNumHeaders + kNumConsumer) {
+        *name = kConsumerHeaders[i - kNumHeaders].name;
+        *src = kConsumerHeaders[i - kNumHeaders].src;
+    } else {
+        const int k = i - kNumHeaders - kNumConsumer;
+        *name = gb300_name(k).c_str();
+        *src = kHeaders[k].src;
+    }
     return true;
 }
 
 uint64_t payload_digest() {
     uint64_t h = fnv1a(std::string("aether_gb300 rtc payload"));
-    for (int i = 0; i < kNumHeaders; ++i) {
-        h = fnv1a(kHeaders[i].name, h);
-        h = fnv1a(kHeaders[i].src, h);
+    for (int i = 0; i < kNumPayload; ++i) {
+        const char *n = nullptr, *src = nullptr;
+        payload_header(i, &n, &src);
+        h = fnv1a(n, h);
+        h = fnv1a(src, h);
     }
     return h;
 }
@@ -120,11 +150,41 @@ uint64_t cache_key(const std::string& source, const std::string& arch, const std
         arch + "|nvrtc" + std::to_string(nvrtc_major) + "." + std::to_string(nvrtc_minor) + "|" + tag;
     uint64_t h = fnv1a(source);
     h = fnv1a(opts_key, h);
-    for (int i = 0; i < kNumHeaders; ++i) {
-        h = fnv1a(kHeaders[i].name, h);
-        h = fnv1a(i == override_index && override_src ? override_src : kHeaders[i].src, h);
+    for (int i = 0; i < kNumPayload; ++i) {
+        const char *n = nullptr, *src = nullptr;
+        payload_header(i, &n, &src);
+        h = fnv1a(n, h);
+        h = fnv1a(i == override_index && override_src ? override_src : src, h);
     }
     return h;
+}
+
+std::string compile_with_payload(const std::string& source, const std::string& arch,
+                                 const std::vector<std::string>& options) {
+    std::vector<const char*> srcs(kNumPayload), names(kNumPayload);
+    for (int i = 0; i < kNumPayload; ++i) payload_header(i, &names[size_t(i)], &srcs[size_t(i)]);
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, source.c_str(), "aether_rtc.cu", kNumPayload, srcs.data(), names.data()) !=
+        NVRTC_SUCCESS)
+        throw std::runtime_error("nvrtcCreateProgram failed");
+    const std::string arch_opt = "--gpu-architecture=" + arch;
+    std::vector<const char*> opts = {arch_opt.c_str(), "--std=c++17"};
+    for (const std::string& o : options) opts.push_back(o.c_str());
+    const nvrtcResult rc = nvrtcCompileProgram(prog, int(opts.size()), opts.data());
+    if (rc != NVRTC_SUCCESS) {
+        size_t n = 0;
+        nvrtcGetProgramLogSize(prog, &n);
+        std::string log(n, '\0');
+        if (n) nvrtcGetProgramLog(prog, &log[0]);
+        nvrtcDestroyProgram(&prog);
+        throw std::runtime_error(std::string("NVRTC compile failed (") + nvrtcGetErrorString(rc) + "):\n" + log);
+    }
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    std::string cubin(n, '\0');
+    nvrtcGetCUBIN(prog, &cubin[0]);
+    nvrtcDestroyProgram(&prog);
+    return cubin;
 }
 
 std::string compile_for_arch(const std::string& source, const std::string& arch) {

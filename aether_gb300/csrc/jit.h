@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 namespace ag {
 
@@ -31,6 +32,12 @@ std::string compile_for_arch(const std::string& source, const std::string& arch)
 int payload_count();
 bool payload_header(int i, const char** name, const char** src);
 uint64_t payload_digest();
+
+// Compile a code generator's `source` for `arch` against the whole payload
+// (the consumer headers included), with extra NVRTC `options`; returns the
+// CUBIN or throws with the NVRTC log.
+std::string compile_with_payload(const std::string& source, const std::string& arch,
+                                 const std::vector<std::string>& options);
 
 // The cache key of `source` compiled for `arch` with option tag `tag` by
 // NVRTC major.minor: the source, the options and every payload header's name

@@ -71,6 +71,7 @@ const AetherGB300V1 kGB300 = {
     aether_plan_generate,
     aether_nvrtc_check,
     aether_plan_cache_key,
+    aether_rtc_compile,
 };
 
 }  // namespace

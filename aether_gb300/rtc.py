@@ -1,11 +1,13 @@
-"""The NVRTC payload (aether_rtc_*): the device headers generated kernels
-include, for kernels a code generator compiles with its own NVRTC program.
+"""The NVRTC payload (aether_rtc_*): the device-safe consumer headers
+(aether/device.h and what it includes) and the engine's device runtime, for
+kernels a code generator compiles with NVRTC.
 
 The counterpart of the reference's sealed header payload
 (dsc/aether_dsc/_core.py:132-200): `payload()` returns the headers by
 include name with a content digest; `Payload.serve()` materialises them in a
 private directory for the lifetime of a `with` block (for compilers that
-read include directories rather than in-memory headers).
+read include directories rather than in-memory headers); `compile()` runs
+NVRTC over a source against the payload and returns the CUBIN.
 """
 
 import contextlib
@@ -30,7 +32,9 @@ class Payload:
         try:
             os.chmod(d, 0o700)
             for name, src in self.headers.items():
-                with open(os.path.join(d, name), "wb") as f:
+                path = os.path.join(d, name)
+                os.makedirs(os.path.dirname(path), mode=0o700, exist_ok=True)
+                with open(path, "wb") as f:
                     f.write(src)
             yield d
         finally:
@@ -50,3 +54,27 @@ def payload():
 def compile_check(source, arch="sm_103a"):
     """NVRTC-compile a kernel that includes the payload headers (no load)."""
     _abi.nvrtc_check(source, arch)
+
+
+def libcudacxx_include():
+    """The CUDA toolkit directory that holds libcu++ (cuda/std/...), which the
+    consumer headers use under NVRTC."""
+    from . import build
+    home = build.cuda_home()
+    for cand in (os.path.join(home, "include", "cccl"), os.path.join(home, "include")):
+        if os.path.isdir(os.path.join(cand, "cuda", "std")):
+            return cand
+    raise RuntimeError("libcu++ (cuda/std) not found under " + home)
+
+
+def compile(source, arch="sm_103a", options=()):
+    """NVRTC-compile `source` against the payload; returns the CUBIN bytes.
+    The libcu++ include path is added for aether/device.h."""
+    L = _abi.lib()
+    opts = ["--include-path=" + libcudacxx_include()] + list(options)
+    arr = (ctypes.c_char_p * len(opts))(*[o.encode() for o in opts])
+    n = ctypes.c_size_t()
+    _abi.check(L.aether_rtc_compile(source.encode(), arch.encode(), arr, len(opts), None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value)
+    _abi.check(L.aether_rtc_compile(source.encode(), arch.encode(), arr, len(opts), buf, n.value, ctypes.byref(n)))
+    return buf.raw[: n.value]

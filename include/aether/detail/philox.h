@@ -11,7 +11,7 @@
 // generated kernels and to the reference's CPU path.
 #pragma once
 
-#include <cstdint>
+#include "aether/detail/std.h"
 
 #include "aether/macros.h"
 

@@ -19,9 +19,7 @@
 // nodes in aether::per_sample (an addition of this engine).
 #pragma once
 
-#include <cstddef>
-#include <type_traits>
-#include <utility>
+#include "aether/detail/std.h"
 
 #include "aether/layout.h"
 #include "aether/math.h"
@@ -88,17 +86,17 @@ inline constexpr bool same_shape = std::is_same<extents_of<A>, extents_of<B>>::v
 
 // Right-nested folds over all components (expr/Reduce.h:149-188): the fold of
 // N terms is f(N-1) + (f(N-2) + (... + f(0))), with no zero seed.
-template <class E, class F, std::size_t... K>
-AETHER_DEVICEANDHOST() constexpr auto fold_sum_(const E& e, const SampleIndex& i, F f, std::index_sequence<K...>) {
+template <class E, std::size_t... K>
+AETHER_DEVICEANDHOST() constexpr auto fold_sum_(const E& e, const SampleIndex& i, std::index_sequence<K...>) {
     using T = typename E::element_type;
     T acc{};
     bool first = true;
-    ((acc = first ? f(evalFlat<K>(e, i)) : T(f(evalFlat<K>(e, i)) + acc), first = false), ...);
+    ((acc = first ? T(evalFlat<K>(e, i)) : T(evalFlat<K>(e, i) + acc), first = false), ...);
     return acc;
 }
-template <class E, class F>
-AETHER_DEVICEANDHOST() constexpr auto fold_sum(const E& e, const SampleIndex& i, F f) {
-    return fold_sum_(e, i, f, std::make_index_sequence<size_of<extents_of<E>>>{});
+template <class E>
+AETHER_DEVICEANDHOST() constexpr auto fold_sum(const E& e, const SampleIndex& i) {
+    return fold_sum_(e, i, std::make_index_sequence<size_of<extents_of<E>>>{});
 }
 template <class L, class R, std::size_t... K>
 AETHER_DEVICEANDHOST() constexpr auto fold_dot_(const L& l, const R& r, const SampleIndex& i, std::index_sequence<K...>) {
@@ -189,7 +187,7 @@ public:
                                     std::make_index_sequence<detail::size_of<detail::extents_of<Derived>>>{});
     }
     AETHER_DEVICEANDHOST() constexpr T sum() const {
-        return detail::fold_sum(derived(), SampleIndex::make(std::size_t(0)), [](T v) { return v; });
+        return detail::fold_sum(derived(), SampleIndex::make(std::size_t(0)));
     }
     AETHER_DEVICEANDHOST() constexpr T trace() const {
         using X = detail::extents_of<Derived>;

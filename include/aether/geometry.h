@@ -243,20 +243,19 @@ class CWiseMul : public Expression<CWiseMul<L, R>, typename L::element_type> {
 };
 
 // sum_k a(Rw, k) b(k[, Cl]) folded right-nested: a0 b0, then a_k b_k + acc.
+template <class A, class B, std::size_t Rw, std::size_t Cl, bool Vec, std::size_t k>
+AETHER_DEVICEANDHOST() constexpr typename A::element_type row_term_(const A& a, const B& b, const SampleIndex& i) {
+    if constexpr (Vec)
+        return at2<Rw, k>(a, i) * at1<k>(b, i);
+    else
+        return at2<Rw, k>(a, i) * at2<k, Cl>(b, i);
+}
 template <class A, class B, std::size_t Rw, std::size_t Cl, bool Vec, std::size_t... K>
 AETHER_DEVICEANDHOST() constexpr auto row_dot_(const A& a, const B& b, const SampleIndex& i, std::index_sequence<K...>) {
     using T = typename A::element_type;
     T acc{};
     bool first = true;
-    auto term = [&](auto kc) {
-        constexpr std::size_t k = decltype(kc)::value;
-        if constexpr (Vec)
-            return T(at2<Rw, k>(a, i) * at1<k>(b, i));
-        else
-            return T(at2<Rw, k>(a, i) * at2<k, Cl>(b, i));
-    };
-    ((acc = first ? term(std::integral_constant<std::size_t, K>{})
-                  : T(term(std::integral_constant<std::size_t, K>{}) + acc),
+    ((acc = first ? row_term_<A, B, Rw, Cl, Vec, K>(a, b, i) : T(row_term_<A, B, Rw, Cl, Vec, K>(a, b, i) + acc),
       first = false),
      ...);
     return acc;

@@ -10,8 +10,7 @@
 // and MatView<T,R,C> are the reference's (aether/aether.h:234-260).
 #pragma once
 
-#include <cstddef>
-#include <type_traits>
+#include "aether/detail/std.h"
 
 #include "aether/view.h"
 

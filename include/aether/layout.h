@@ -11,10 +11,7 @@
 // Every member is usable in device code (AETHER_DEVICEHOST) and in host code.
 #pragma once
 
-#include <cstddef>
-#include <cstdint>
-#include <type_traits>
-#include <utility>
+#include "aether/detail/std.h"
 
 #include "aether/macros.h"
 

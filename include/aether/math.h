@@ -20,7 +20,9 @@
 // Every function is usable from device and host code.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <cmath>
+#endif
 
 #include "aether/macros.h"
 
@@ -78,10 +80,12 @@ __device__ inline double sqrt(double x) { return __dsqrt_rn(x); }
 __device__ inline float sqrt(float x) { return __fsqrt_rn(x); }
 }  // namespace dev
 #endif
+#if !defined(__CUDACC_RTC__)
 namespace host {
 template <class T>
 inline T rsqrt(T x) { return T(1) / std::sqrt(x); }
 }  // namespace host
+#endif
 
 AETHER_MATH1(sqrt, AETHER_GB300_D(emu::sqrt, dev::sqrt), dev::sqrt, std::sqrt)
 AETHER_MATH1(rsqrt, AETHER_GB300_D(emu::rsqrt, dev::rsqrt), dev::rsqrt, host::rsqrt)

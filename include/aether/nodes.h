@@ -17,8 +17,7 @@
 // to the engine's aether-ir/1 (gb300_ir) for the fused whole-view launch.
 #pragma once
 
-#include <cstddef>
-#include <type_traits>
+#include "aether/detail/std.h"
 
 #include "aether/expression.h"
 
@@ -391,7 +390,7 @@ public:
         if constexpr (Kind == 1) return fold_dot(l_, l_, i);
         if constexpr (Kind == 2) return math::sqrt(fold_dot(l_, l_, i));
         if constexpr (Kind == 3) return math::rsqrt(fold_dot(l_, l_, i));
-        if constexpr (Kind == 4) return fold_sum(l_, i, [](element_type v) { return v; });
+        if constexpr (Kind == 4) return fold_sum(l_, i);
         if constexpr (Kind == 5)
             return fold_maxabs_(l_, i, std::make_index_sequence<size_of<extents_of<L>>>{});
     }

@@ -18,10 +18,7 @@
 // each; float draws use the float conversions.
 #pragma once
 
-#include <cstdint>
-#include <memory>
-#include <string>
-#include <vector>
+#include "aether/detail/std.h"
 
 #include "aether/detail/philox.h"
 #include "aether/item.h"
@@ -60,6 +57,15 @@ AETHER_DEVICEANDHOST() inline Real drawNormal(std::uint64_t key, std::uint32_t g
 }
 
 #if AETHER_GB300_HOST_IR
+}  // namespace detail
+}  // namespace random
+}  // namespace aether
+#include <memory>
+#include <string>
+#include <vector>
+namespace aether {
+namespace random {
+namespace detail {
 /** The aether-ir/1 leaf the engine's kernels regenerate. N(0, 1) (and
  *  lognormal(0, 1)) keeps its parameters as literals, so the kernel skips the
  *  affine step 0 + 1 z, which is z bit for bit (a Box-Muller draw is never 0). */

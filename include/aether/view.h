@@ -18,9 +18,7 @@
 // device code (view/View.h:281-286).
 #pragma once
 
-#include <cstddef>
-#include <type_traits>
-#include <utility>
+#include "aether/detail/std.h"
 
 #include "aether/expression.h"
 #include "aether/layout.h"
@@ -171,20 +169,21 @@ AETHER_DEVICEANDHOST() constexpr decltype(auto) eval_ref_(const V& v, const Samp
     return v(unflat<X>(K, D)..., i.global());
 }
 
-template <int Op, class V, class E, std::size_t... K>
-AETHER_DEVICEANDHOST() constexpr void assign_sample_(const V& v, const SampleIndex& i, const E& e,
-                                                  std::index_sequence<K...>) {
+template <int Op, std::size_t K, class V, class E>
+AETHER_DEVICEANDHOST() constexpr void assign_one_(const V& v, const SampleIndex& i, const E& e) {
     using X = typename V::element_extents;
     using T = typename V::value_type;
-    auto one = [&](auto kc) {
-        constexpr std::size_t k = decltype(kc)::value;
-        auto&& ref = eval_ref_<X, k>(v, i, std::make_index_sequence<X::Rank>{});
-        const T val = static_cast<T>(evalFlat<k>(e, i));
-        if constexpr (Op == 0) ref = val;
-        if constexpr (Op == 1) ref = ref + val;
-        if constexpr (Op == 2) ref = ref - val;
-    };
-    (one(std::integral_constant<std::size_t, K>{}), ...);
+    auto&& ref = eval_ref_<X, K>(v, i, std::make_index_sequence<X::Rank>{});
+    const T val = static_cast<T>(evalFlat<K>(e, i));
+    if constexpr (Op == 0) ref = val;
+    if constexpr (Op == 1) ref = ref + val;
+    if constexpr (Op == 2) ref = ref - val;
+}
+
+template <int Op, class V, class E, std::size_t... K>
+AETHER_DEVICEANDHOST() constexpr void assign_sample_(const V& v, const SampleIndex& i, const E& e,
+                                                     std::index_sequence<K...>) {
+    (assign_one_<Op, K>(v, i, e), ...);
 }
 
 }  // namespace detail

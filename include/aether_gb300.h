@@ -343,17 +343,29 @@ int aether_runtime_eval(int op, const AetherRuntimeView* a, const AetherRuntimeV
  * length into `len`. Stands in for the reference's compile-time type check of
  * an expression (the static_asserts of the expr/nodes headers and expr/Assign.h:205-231). */
 int aether_plan_generate(const char* ir, const AetherLowering* lowering, char* buf, size_t cap, size_t* len);
-/* The NVRTC payload: the device headers every generated kernel includes
- * (ag_device.cuh: Philox streams, word conversions, native math facade,
- * compensated-sum primitives; ag_emu64.cuh and its tables: the double-float
- * arithmetic and functions), for kernels a code generator compiles with its own
- * NVRTC program and that call the engine's device functions. Replaces the
- * sealed header payload of dsc/aether_dsc/_core.py:132-200 (names, bytes and a
- * content digest) over the NVRTC-parseable surface of aether/device.h.
- * Sources are NUL-terminated, owned by the library, valid until unload. */
+/* The NVRTC payload, for kernels a code generator compiles with NVRTC.
+ * Replaces the sealed header payload of dsc/aether_dsc/_core.py:132-200
+ * (names, bytes and a content digest) over the NVRTC-parseable surface of
+ * aether/device.h (aether/device.h:1-30). It holds, each under its include
+ * name: the device-safe consumer headers "aether/device.h" and everything it
+ * includes (views, SampleIndex, Items, expressions, aether::math, Philox
+ * leaves), and the engine's device runtime (ag_device.cuh: Philox streams,
+ * word conversions, native math facade, compensated sums; ag_emu64.cuh and
+ * its tables: double-float arithmetic and functions; the Box-Muller draw),
+ * under its bare names and again under "aether/gb300/". Sources are
+ * NUL-terminated, owned by the library, valid until unload. The digest covers
+ * every name and byte. */
 int aether_rtc_header_count(void);
 int aether_rtc_header(int index, const char** name, const char** source);
 uint64_t aether_rtc_digest(void);
+/* Compile `source` for `arch` (e.g. "sm_103a") with NVRTC against the whole
+ * payload, plus `n_options` extra NVRTC options (for aether/device.h under
+ * NVRTC: --include-path=<CUDA>/include/cccl, where the toolkit keeps libcu++;
+ * -DAETHER_GB300_EMULATED_FP64 for the double-float math facade). Writes the
+ * CUBIN into `cubin` (`cap` bytes) and its size into `len`; with cubin NULL
+ * only the size. On failure the NVRTC log is the last error. */
+int aether_rtc_compile(const char* source, const char* arch, const char* const* options, int n_options, void* cubin,
+                       size_t cap, size_t* len);
 /* The in-memory and on-disk cache key of a generated kernel: `source` compiled
  * for `arch` under option tag `tag` by this library's NVRTC, hashed with the
  * name and text of every payload header above, so a kernel cached before any
@@ -440,6 +452,8 @@ typedef struct AetherGB300V1 {
     int (*nvrtc_check)(const char* source, const char* arch);
     int (*plan_cache_key)(const char* source, const char* arch, const char* tag, int header_index,
                           const char* header_source, uint64_t* key);
+    int (*rtc_compile)(const char* source, const char* arch, const char* const* options, int n_options, void* cubin,
+                       size_t cap, size_t* len);
 } AetherGB300V1;
 const AetherGB300V1* aether_gb300_v1(void);
 

@@ -193,7 +193,7 @@ def test_gb300_table_binds_every_path_entry():
              "batch_set_items", "batch_launch", "batch_capture", "batch_replay", "batch_info", "batch_release",
              "serve_open", "serve_submit", "serve_feed", "serve_status", "serve_wait", "serve_release", "serve_stats",
              "serve_close", "runtime_eval", "rtc_header_count", "rtc_header", "rtc_digest", "plan_generate",
-             "nvrtc_check", "plan_cache_key"]
+             "nvrtc_check", "plan_cache_key", "rtc_compile"]
 
     class T(ctypes.Structure):
         _fields_ = [("abi", ctypes.c_uint32), ("memory", P)] + [(n, P) for n in names]

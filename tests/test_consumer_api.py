@@ -145,7 +145,7 @@ def _run_kernels(tmp_path, exe, n):
     res, off = {}, 0
     for name, comps in (("a", 3), ("b", 3), ("c", 3), ("d0", 3), ("q", 4), ("m", 9), ("d1", 3), ("d2", 3), ("cr", 3),
                         ("cr2", 3), ("qr", 3), ("mi", 9), ("dt", 1)):
-        res[name] = raw[off:off + comps * cap].reshape(comps, cap)[:, :n]
+        res[name] = np.ascontiguousarray(raw[off:off + comps * cap].reshape(comps, cap)[:, :n])
         off += comps * cap
     assert off == raw.size
     return res
