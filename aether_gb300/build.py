@@ -37,7 +37,7 @@ EMBED = [("kAgDeviceSrc", "ag_device.cuh"), ("kAgEmu64Src", "ag_emu64.cuh"),
 # exported with the engine's device runtime as the NVRTC payload for code
 # generators, each under its include name.
 CONSUMER_HEADERS = ["macros.h", "detail/std.h", "layout.h", "math.h", "expression.h", "nodes.h", "geometry.h",
-                    "view.h", "item.h", "detail/philox.h", "random.h", "device.h"]
+                    "view.h", "item.h", "bundle.h", "detail/philox.h", "random.h", "device.h"]
 EXPORT_PREFIX = "aether_"
 
 

@@ -327,6 +327,7 @@ def secondary_config3(ag, n=1 << 27):
     s32, s64 = red32.cpu().tolist(), red64.cpu().tolist()
     res["global_sum_rel_diff"] = abs((s32[0] + s32[1]) - (s64[0] + s64[1])) / abs(s64[0] + s64[1])
     res["speedup_vs_fp64"] = round(best / ms32, 3)
+    res["speedup_vs_native_fp64"] = round(res["f64_native_ms"] / ms32, 3)
     res["gbs_ff"] = round(n * 68 / (ms32 * 1e-3) / 1e9, 1)
     del x64, y64, d64, d32
     torch.cuda.empty_cache()
@@ -376,9 +377,11 @@ def config3_expressions(ag, n):
         del ins
         d64 = ag.Array("f64", (3,), n)
         best = None
+        per = {}
         for m in (0, 1):
             L64 = ag.prepare(d64, fn([x.view() for x in ins64]), math=m)
             ms = _time_ms(L64)
+            per[m] = ms
             best = ms if best is None else min(best, ms)
         ag.prepare(d64, fn([x.view() for x in ins64]), math=0)()   # FP64 reference values
         torch.cuda.synchronize()
@@ -387,6 +390,8 @@ def config3_expressions(ag, n):
         rel = torch.abs(v - ref) / torch.clamp(torch.abs(ref), min=1e-300)
         finite = torch.isfinite(ref)
         out[name] = {"ff_ms": round(ms_ff, 4), "f64_ms": round(best, 4), "speedup_vs_fp64": round(best / ms_ff, 3),
+                     "f64_native_ms": round(per[0], 4), "f64_emulated_ms": round(per[1], 4),
+                     "speedup_vs_native_fp64": round(per[0] / ms_ff, 3), "kernel": Lff.plan.name,
                      "ff_samples_per_s": round(n / (ms_ff * 1e-3), 1), "bytes_per_sample_ff": bff,
                      "bytes_per_sample_f64": b64, "max_rel_err_vs_fp64": float(torch.max(rel[finite]).item()),
                      "median_rel_err_vs_fp64": float(torch.median(rel[finite]).item())}

@@ -33,6 +33,7 @@
 #include "aether/geometry.h"
 #include "aether/view.h"
 #include "aether/item.h"
+#include "aether/bundle.h"
 #include "aether/random.h"
 #include "aether/array.h"
 #include "aether/eval.h"

@@ -22,5 +22,6 @@
 #include "aether/geometry.h"
 #include "aether/view.h"
 #include "aether/item.h"
+#include "aether/bundle.h"
 #include "aether/detail/philox.h"
 #include "aether/random.h"

@@ -34,6 +34,10 @@ template <class V>
 class ConstSampleRef;
 template <class T, std::size_t... Es>
 class Item;
+template <std::size_t W>
+struct BundleIndex;
+template <class V, std::size_t W>
+class BundleRef;
 
 #if AETHER_GB300_HOST_IR
 // The engine's whole-view assignment (aether/eval.h): dst <op>= e as one kernel.
@@ -133,6 +137,9 @@ public:
     AETHER_DEVICEANDHOST() constexpr ConstSampleRef<const View> operator[](const SampleIndex& i) const {
         return ConstSampleRef<const View>(*this, i);
     }
+    /** W consecutive samples (aether/bundle.h). */
+    template <std::size_t W>
+    AETHER_DEVICEANDHOST() constexpr BundleRef<View, W> operator[](const BundleIndex<W>& bi);
 
 #if AETHER_GB300_HOST_IR
     /** Host: every sample of this device view <- e, as one engine kernel. */

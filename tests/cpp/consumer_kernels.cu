@@ -91,6 +91,14 @@ void geometryKernel(Strided3 a, Strided3 b, Strided4 q, Strided33 m, Strided3 cr
     dt(i.global()) = x.dot(y);
 }
 
+/** The plain fused assignment again, two samples per thread (BundleIndex). */
+AETHER_KERNEL()
+void cfg1BundleKernel(Strided3 a, Strided3 b, Strided3 c, Strided3 d) {
+    const aether::BundleIndex<2> bi = aether::BundleIndex<2>::make(threadIdx.x, blockIdx.x, blockDim.x);
+    if (!bi.mask(d.samples()).lane(0)) return;
+    d[bi] = a + b * c + aether::cwiseSin(a) * aether::cwiseExp((c * c) * (-1.0));
+}
+
 template <class A>
 void write(std::FILE* f, A& arr) {
     arr.download();
@@ -120,6 +128,10 @@ int main(int argc, char** argv) {
     aether::cuda::checkLastLaunch("fillKernel");
     cfg1Kernel<<<cfg.blocks, cfg.threads>>>(a.deviceView(), b.deviceView(), c.deviceView(), d1.deviceView());
     aether::cuda::checkLastLaunch("cfg1Kernel");
+    Array<double, 3> d1b(n);
+    const auto cfgb = aether::cuda::bundleLaunchConfig(n, 2, 128);
+    cfg1BundleKernel<<<cfgb.blocks, cfgb.threads>>>(a.deviceView(), b.deviceView(), c.deviceView(), d1b.deviceView());
+    aether::cuda::checkLastLaunch("cfg1BundleKernel");
     cfg2aKernel<<<cfg.blocks, cfg.threads>>>(a.deviceView(), b.deviceView(), c.deviceView(), d0.deviceView(),
                                              d2.deviceView());
     aether::cuda::checkLastLaunch("cfg2aKernel");
@@ -191,6 +203,17 @@ int main(int argc, char** argv) {
     write(f, mi);
     write(f, dt);
     std::fclose(f);
+    d1b.download();
+    {
+        auto x1 = d1.hostView();
+        auto x2 = d1b.hostView();
+        for (std::size_t k = 0; k < n; ++k)
+            for (int j = 0; j < 3; ++j)
+                if (x1(j, k) != x2(j, k)) {
+                    std::printf("bundle assignment differs at sample %zu\n", k);
+                    return 1;
+                }
+    }
     if (std::memcmp(cr.hostView().data(), cr2.hostView().data(), 3 * cr.capacity() * sizeof(double)) != 0) {
         std::printf("cross: view and Item forms differ\n");
         return 1;
