@@ -12,6 +12,7 @@
 // uncaptured launch; Item and view forms of cross identical) pass.
 #include <aether/aether.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -180,11 +181,17 @@ int main(int argc, char** argv) {
     AETHER_CHECK_CUDA(cudaStreamDestroy(stream));
     {
         auto uh = outU.hostView();
-        for (std::size_t k = 0; k < kN; ++k)
-            if (uh(k) != (double(k) * 0.21 - 4.0) + 2.25 * (double(k) * 0.05 + 1.0)) {
+        auto xh = x.hostView();
+        auto yh = y.hostView();
+        for (std::size_t k = 0; k < kN; ++k) {
+            // a + s*b with or without FMA contraction, as the kernel was compiled
+            volatile double prod = 2.25 * yh(k);
+            const double separate = xh(k) + prod, fused = std::fma(2.25, yh(k), xh(k));
+            if (uh(k) != separate && uh(k) != fused) {
                 std::printf("axpy value at %zu\n", k);
                 return 1;
             }
+        }
     }
 
     std::FILE* f = std::fopen(argv[1], "wb");
