@@ -53,7 +53,7 @@ class AetherBatchInfo(ctypes.Structure):
 class AetherServeConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("mode", ctypes.c_int), ("max_inflight", ctypes.c_int),
                 ("max_items", ctypes.c_int), ("block", ctypes.c_int), ("ipt", ctypes.c_int),
-                ("idle_spin_us", ctypes.c_int), ("upload_engine", ctypes.c_int)]
+                ("idle_spin_us", ctypes.c_int), ("upload_engine", ctypes.c_int), ("grouping", ctypes.c_int)]
 
 
 class AetherServeOperand(ctypes.Structure):

@@ -168,7 +168,8 @@ struct Server {
     int dev = 0, sms = 1;
     AetherServeConfig cfg{};
     std::vector<PlanObj*> plans;
-    BatchObj* batch = nullptr;
+    BatchObj* batch = nullptr;              // every plan behind a switch (grouping 1)
+    std::vector<BatchObj*> plan_batch;      // one work-list kernel per plan (grouping 0)
     char* base = nullptr;
     Arena arena;
     cudaStream_t copy_stream = nullptr;
@@ -350,23 +351,75 @@ struct Server {
     // Launch requests [first, first + count) of a slot on its stream, then
     // their host output copies. One request runs its plan's own kernel (no
     // work list, same arithmetic); several run as one batched kernel.
+    // One request through its plan's own kernel.
+    void launch_plain(const Request& r, cudaStream_t stream, std::vector<AetherOperand>& ops) {
+        PlanObj* P = plans[size_t(r.plan)];
+        AetherLaunch a = launch_of(r, ops);
+        AgArgsHost k;
+        const bool vect = make_args(P, &a, k) && P->vec > 1;
+        const uint64_t per = chunk_samples(*P, vect);
+        const int bps = vect ? P->blocks_per_sm_v : P->blocks_per_sm_s;
+        const uint64_t cap = uint64_t(std::max(bps, 1)) * uint64_t(P->sms);
+        const unsigned grid = unsigned(std::max<uint64_t>(1, std::min((r.n + per - 1) / per, cap)));
+        void* params[] = {&k};
+        ag_ck(cudaLaunchKernel(reinterpret_cast<const void*>(vect ? P->fv : P->fs), dim3(grid),
+                               dim3(unsigned(P->low.block)), params, 0, stream),
+              "cudaLaunchKernel(plain)");
+    }
+
     void launch_group(Slot& S, size_t first, size_t count) {
         if (!count) return;
         std::vector<AetherOperand> ops;
         if (count == 1) {
-            const Request& r = *S.rs[first];
-            PlanObj* P = plans[size_t(r.plan)];
-            AetherLaunch a = launch_of(r, ops);
-            AgArgsHost k;
-            const bool vect = make_args(P, &a, k) && P->vec > 1;
-            const uint64_t per = chunk_samples(*P, vect);
-            const int bps = vect ? P->blocks_per_sm_v : P->blocks_per_sm_s;
-            const uint64_t cap = uint64_t(std::max(bps, 1)) * uint64_t(P->sms);
-            const unsigned grid = unsigned(std::max<uint64_t>(1, std::min((r.n + per - 1) / per, cap)));
-            void* params[] = {&k};
-            ag_ck(cudaLaunchKernel(reinterpret_cast<const void*>(vect ? P->fv : P->fs), dim3(grid),
-                                   dim3(unsigned(P->low.block)), params, 0, S.stream),
-                  "cudaLaunchKernel(plain)");
+            launch_plain(*S.rs[first], S.stream, ops);
+        } else if (!plan_batch.empty()) {
+            // grouped by plan (the caller sorted the range): one work list,
+            // copied once, and one launch per plan -- its own kernel for a
+            // lone request, the plan's work-list kernel for several
+            size_t b = 0;
+            std::vector<std::pair<size_t, uint64_t>> runs;   // (end of run, tiles)
+            while (b < count) {
+                const int plan = S.rs[first + b]->plan;
+                const BatchObj& B = *plan_batch[size_t(plan)];
+                size_t e = b;
+                uint64_t tiles = 0;
+                while (e < count && S.rs[first + e]->plan == plan) {
+                    const Request& r = *S.rs[first + e];
+                    AgItemHost& h = S.staging[first + e];
+                    h = AgItemHost{};
+                    AetherLaunch a = launch_of(r, ops);
+                    make_args(B.plans[0], &a, h.a);   // alignment was checked at submit
+                    h.tile0 = tiles;
+                    h.plan = 0;
+                    const uint64_t per = batch_tile_samples(B, 0);
+                    tiles += (r.n + per - 1) / per;
+                    ++e;
+                }
+                runs.push_back({e, tiles});
+                b = e;
+            }
+            AgItemHost* dev = static_cast<AgItemHost*>(S.dev_items) + first;
+            if (runs.size() < count)
+                ag_ck(cudaMemcpyAsync(dev, S.staging + first, count * sizeof(AgItemHost), cudaMemcpyHostToDevice,
+                                      S.stream),
+                      "cudaMemcpyAsync(work list)");
+            b = 0;
+            for (const auto& run : runs) {
+                const size_t e = run.first;
+                if (e - b == 1) {
+                    launch_plain(*S.rs[first + b], S.stream, ops);
+                } else {
+                    const BatchObj& B = *plan_batch[size_t(S.rs[first + b]->plan)];
+                    void* items = dev + b;
+                    int n = int(e - b);
+                    uint64_t t = run.second;
+                    void* params[] = {&items, &n, &t};
+                    ag_ck(cudaLaunchKernel(reinterpret_cast<const void*>(B.kernel), dim3(batch_grid(B, t)),
+                                           dim3(unsigned(B.block)), params, 0, S.stream),
+                          "cudaLaunchKernel(batch)");
+                }
+                b = e;
+            }
         } else {
             uint64_t tiles = 0;
             for (size_t i = 0; i < count; ++i) {
@@ -513,6 +566,12 @@ struct Server {
                     });
                     const size_t ready = size_t(mid - S->rs.begin());
                     S->n_first = (ready > 0 && ready < S->rs.size()) ? ready : 0;
+                    if (!plan_batch.empty()) {
+                        // each launch group ordered by plan: one run per plan
+                        auto by_plan = [](const Request* x, const Request* y) { return x->plan < y->plan; };
+                        std::stable_sort(S->rs.begin(), mid, by_plan);
+                        std::stable_sort(mid, S->rs.end(), by_plan);
+                    }
                     S->first_retired = false;
                     S->busy = true;
                     // The completion of a slot that waited for the copy stream
@@ -721,6 +780,7 @@ void destroy(Server* S) {
     }
     if (S->base) cudaFree(S->base);
     if (S->batch) aether_batch_release(S->batch);
+    for (BatchObj* b : S->plan_batch) aether_batch_release(b);
     cudaGetLastError();
     cudaSetDevice(prev);
     delete S;
@@ -756,9 +816,19 @@ AG_EXPORT int aether_serve_open(void* const* plans, int n_plans, const AetherSer
         AetherLowering low{};
         low.block = S->cfg.block;
         low.ipt = S->cfg.ipt;
-        void* b = nullptr;
-        if (aether_batch_create(plans, n_plans, &low, &b) != AETHER_OK) throw std::runtime_error(aether_last_error());
-        S->batch = static_cast<BatchObj*>(b);
+        if (S->cfg.grouping != 0 && S->cfg.grouping != 1) throw std::runtime_error("serve_open: grouping must be 0 or 1");
+        if (S->cfg.mode == AETHER_SERVE_BATCHED && S->cfg.grouping == 0) {
+            for (int p = 0; p < n_plans; ++p) {
+                void* b = nullptr;
+                if (aether_batch_create(&plans[p], 1, &low, &b) != AETHER_OK)
+                    throw std::runtime_error(aether_last_error());
+                S->plan_batch.push_back(static_cast<BatchObj*>(b));
+            }
+        } else {
+            void* b = nullptr;
+            if (aether_batch_create(plans, n_plans, &low, &b) != AETHER_OK) throw std::runtime_error(aether_last_error());
+            S->batch = static_cast<BatchObj*>(b);
+        }
         void* base = nullptr;
         ag_ck(cudaMalloc(&base, S->cfg.hbm_budget_bytes), "cudaMalloc(serving arena)");
         S->base = static_cast<char*>(base);

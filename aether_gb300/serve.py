@@ -170,11 +170,12 @@ class Server:
     """aether_serve_open over `shapes` (ShapeTemplate list)."""
 
     def __init__(self, shapes, budget_bytes, mode="batched", max_inflight=0, max_items=0, block=0, ipt=0,
-                 idle_spin_us=0, upload_engine="gather"):
+                 idle_spin_us=0, upload_engine="gather", grouping="per_plan"):
         self.shapes = list(shapes)
         arr = (ctypes.c_void_p * len(self.shapes))(*[s.plan.handle for s in self.shapes])
         cfg = _abi.AetherServeConfig(int(budget_bytes), MODES[mode], max_inflight, max_items, block, ipt,
-                                     idle_spin_us, {"gather": 0, "copy": 1}[upload_engine])
+                                     idle_spin_us, {"gather": 0, "copy": 1}[upload_engine],
+                                     {"per_plan": 0, "mixed": 1}[grouping])
         h = ctypes.c_void_p()
         _abi.check(_abi.lib().aether_serve_open(arr, len(self.shapes), ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h

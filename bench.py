@@ -462,8 +462,8 @@ def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, satu
     shapes = serve.standard_shapes()
     pools = serve.HostPools()
 
-    def run(mode, trace):
-        with serve.Server(shapes, budget, mode=mode) as srv:
+    def run(mode, trace, grouping="per_plan"):
+        with serve.Server(shapes, budget, mode=mode, grouping=grouping) as srv:
             reqs = []
             for s, n, ids, t in trace:
                 sh = shapes[s]
@@ -502,6 +502,13 @@ def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, satu
         trace = serve.make_trace(shapes, saturation_requests, None, seed=7, reuse=reuse)
         b, p = run("batched", trace), run("plain", trace)
         res[name] = {"batched": b, "plain": p, "speedup_req_per_s": round(b["req_per_s"] / p["req_per_s"], 2)}
+        if reuse == 1.0:
+            # the same trace through one work-list kernel holding every plan
+            m = run("batched", trace, grouping="mixed")
+            res[name]["batched_one_kernel"] = m
+            res[name]["speedup_one_kernel_req_per_s"] = round(m["req_per_s"] / p["req_per_s"], 2)
+    res["grouping"] = ("a launch's requests grouped by plan, one work-list kernel per plan "
+                       "(a lone request runs its plan's own kernel)")
     return res
 
 
@@ -783,13 +790,16 @@ def run_ours(args):
     if not args.no_secondary:
         # the other configurations, measured after the timed region
         secondary = {}
-        if math_mode != 0:
+        wanted = set(args.secondary.split(",")) if args.secondary else None
+        if math_mode != 0 and (wanted is None or "native_fp64_step" in wanted):
             try:
                 secondary["native_fp64_step"] = native_fp64_step(ag, arrs, d, z, expr, g, args.steps, stream, ref)
             except Exception as ex:   # reported, never hidden
                 secondary["native_fp64_step"] = {"error": str(ex).splitlines()[0][:300] if str(ex) else repr(ex)}
         for name, fn in (("config1_plain", secondary_config1), ("config3_precision_form", secondary_config3),
                          ("config4_batch", secondary_config4), ("config5_serving", secondary_config5)):
+            if wanted is not None and name not in wanted:
+                continue
             try:
                 secondary[name] = fn(ag)
             except Exception as ex:   # reported, never hidden
@@ -826,6 +836,9 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default lowering instead of the autotuned one")
     ap.add_argument("--no-secondary", action="store_true", help="skip configs 1, 3, 4 and 5 after the timed region")
     ap.add_argument("--e2e-chunks", type=int, default=4, help="sample blocks of the pipelined end-to-end step")
+    ap.add_argument("--secondary", default="", help="comma-separated subset of the secondary measurements "
+                                                     "(native_fp64_step, config1_plain, config3_precision_form, "
+                                                     "config4_batch, config5_serving); default all")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
     args = ap.parse_args()

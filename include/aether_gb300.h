@@ -239,6 +239,9 @@ typedef struct AetherServeConfig {
     int idle_spin_us;          /* the loop polls this long after its last work before it sleeps; 0 = 2000 */
     int upload_engine;         /* 0: SMs read mapped pinned host operands in one gather kernel per launch
                                   (other memory: copy engine); 1: copy engine only */
+    int grouping;              /* batched mode: 0 = the requests of a launch grouped by plan, one work-list
+                                  kernel compiled for each plan (a lone request runs its plan's own kernel);
+                                  1 = one work-list kernel holding every plan behind a switch */
 } AetherServeConfig;
 
 typedef struct AetherServeOperand {

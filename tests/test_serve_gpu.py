@@ -99,6 +99,11 @@ def test_same_alone_in_mix_and_plain(shapes, pools):
     copied, _, _ = _mixed(shapes, pools, trace, max_items=64, upload_engine="copy")
     for a, c in zip(alone, copied):
         assert torch.equal(a, c)
+    # one kernel holding every plan instead of one work-list kernel per plan
+    one, osts, _ = _mixed(shapes, pools, trace, max_items=64, grouping="mixed")
+    assert max(s["launch_items"] for s in osts) > 1
+    for a, o in zip(alone, one):
+        assert torch.equal(a, o)
     assert stats["resident_hits"] > 0 and stats["completed"] == len(trace)
 
 
