@@ -284,11 +284,15 @@ def secondary_config1(ag):
     return out
 
 
-def secondary_config3(ag, n=1 << 27):
+PRECISION_LOG2 = 27
+
+
+def secondary_config3(ag, n=None):
     """Config 3 (precision form): per-sample dot of two Array<float,8> plus one
     global sum, FP32 storage with float-float working values, against the same
     workload in FP64 storage (best of the native and emulated FP64 lowerings)."""
     import torch
+    n = n or (1 << PRECISION_LOG2)
     g = ag.Generator(3)
 
     def loguniform(arr, k):
@@ -841,9 +845,11 @@ def main():
                                                      "config4_batch, config5_serving); default all")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")
+    ap.add_argument("--precision-log2", type=int, default=27, help="log2 samples of the precision-form parts")
     args = ap.parse_args()
-    global N_EXPR, N_FILL, BYTES_EXPR, BYTES_FILL
+    global N_EXPR, N_FILL, BYTES_EXPR, BYTES_FILL, PRECISION_LOG2
     N_EXPR, N_FILL = 1 << args.expr_log2, 1 << args.fill_log2
+    PRECISION_LOG2 = args.precision_log2
     BYTES_EXPR, BYTES_FILL = N_EXPR * 120, N_FILL * 8
     if args.impl == "reference":
         return run_reference(args)
