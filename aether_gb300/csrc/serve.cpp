@@ -547,17 +547,23 @@ struct Server {
             lk.lock();
             retire(fin, t_fin);
             Slot* S = nullptr;
+            size_t free_slots = 0;
             for (Slot& sl : slots)
                 if (!sl.busy) {
-                    S = &sl;
-                    break;
+                    if (!S) S = &sl;
+                    ++free_slots;
                 }
             bool blocked = false;
             if (S && !queue.empty() && fatal.empty()) {
                 std::vector<Upload> ups;
                 bool wait_uploads = false;
                 const uint64_t ta = now();
-                blocked = admit(*S, limit, ups, wait_uploads);
+                // Spread what waits over the free slots: requests run side by
+                // side on separate streams while slots are free (a light load
+                // launches them one by one, as plain mode does), and share
+                // launches only once the queue outgrows the free slots.
+                const size_t share = (queue.size() + free_slots - 1) / free_slots;
+                blocked = admit(*S, std::min(limit, std::max<size_t>(1, share)), ups, wait_uploads);
                 st.admit_ns += now() - ta;
                 if (!S->rs.empty()) {
                     // requests that read resident operands only go first

@@ -466,8 +466,8 @@ def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, satu
     shapes = serve.standard_shapes()
     pools = serve.HostPools()
 
-    def run(mode, trace, grouping="per_plan"):
-        with serve.Server(shapes, budget, mode=mode, grouping=grouping) as srv:
+    def run(mode, trace, grouping="per_plan", **kw):
+        with serve.Server(shapes, budget, mode=mode, grouping=grouping, **kw) as srv:
             reqs = []
             for s, n, ids, t in trace:
                 sh = shapes[s]
@@ -507,10 +507,18 @@ def secondary_config5(ag, rates=SERVE_RATES, seconds=1.0, budget=120 << 30, satu
         b, p = run("batched", trace), run("plain", trace)
         res[name] = {"batched": b, "plain": p, "speedup_req_per_s": round(b["req_per_s"] / p["req_per_s"], 2)}
         if reuse == 1.0:
-            # the same trace through one work-list kernel holding every plan
+            # the same trace through one work-list kernel holding every plan,
+            # and with other launch sizes and slot counts
             m = run("batched", trace, grouping="mixed")
             res[name]["batched_one_kernel"] = m
             res[name]["speedup_one_kernel_req_per_s"] = round(m["req_per_s"] / p["req_per_s"], 2)
+            sweep = {}
+            for items, inflight in ((1024, 4), (1024, 8), (4096, 4)):
+                r = run("batched", trace, max_items=items, max_inflight=inflight)
+                sweep["items%d_slots%d" % (items, inflight)] = {k: r[k] for k in (
+                    "req_per_s", "gbs", "launches", "items_per_launch", "enqueue_us_per_launch",
+                    "admit_us_per_launch", "p50_us", "p99_us")}
+            res[name]["batched_sweep"] = sweep
     res["grouping"] = ("a launch's requests grouped by plan, one work-list kernel per plan "
                        "(a lone request runs its plan's own kernel)")
     return res
