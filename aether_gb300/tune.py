@@ -42,10 +42,17 @@ def _device_name():
 
 
 def _code_digest():
-    """Digest of the device code every kernel includes: a tuning result stays
-    valid only for the code it was measured on."""
-    from . import _abi
-    return "%016x" % _abi.lib().aether_rtc_digest()
+    """Digest of the device runtime every generated kernel includes (the
+    payload headers under their bare names; the consumer headers under
+    aether/ never reach a generated kernel): a tuning result stays valid only
+    for the code it was measured on."""
+    from . import rtc
+    h = hashlib.sha1()
+    for name, src in sorted(rtc.payload().headers.items()):
+        if not name.startswith("aether/"):
+            h.update(name.encode())
+            h.update(src)
+    return h.hexdigest()[:16]
 
 
 def _generated_digest(ir, math, contract):

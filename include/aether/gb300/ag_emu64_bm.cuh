@@ -34,14 +34,22 @@ __device__ AG_NOINLINE df from_u54_2m54_any(ag_u64 w, ag_u32 sgn) {
 }
 // The same in 32-bit words when w >= 2^32 (all but 2^-22 of the draws: the
 // normalising shift stays below 32), the general form out of line otherwise.
+// No integer-to-float conversion unit: the head's float is assembled from
+// its bits (the top 24 bits of w << lz are its significand, the shift gives
+// its exponent), and the tail is the next 23 bits made exact by the 2^23
+// exponent trick (one OR and one subtraction) and scaled; the 7 bits below
+// are dropped, 2^-47 of u.
 __device__ __forceinline__ df from_u54_2m54(ag_u64 w, ag_u32 sgn) {
     const ag_u32 hi = (ag_u32)(w >> 32), lo = (ag_u32)w;
     if (hi == 0u) return from_u54_2m54_any(w, sgn);
     const int lz = __clz((int)hi) - 10;   // 0 .. 21
     const ag_u32 nh = __funnelshift_l(lo, hi, (unsigned)lz), nl = lo << lz;   // w << lz in [2^53, 2^54)
-    const ag_u32 sc = ((ag_u32)(103 - lz) << 23) | sgn;
-    const float h = __fmul_rn(__uint2float_rn(__funnelshift_l(nl, nh, 2u)), __int_as_float(sc));   // top 24 bits
-    const float l = __fmul_rn(__uint2float_rn(nl & 0x3fffffffu), __int_as_float(sc - (30u << 23)));
+    const ag_u32 top = __funnelshift_l(nl, nh, 2u);                           // bits 53..30, in [2^23, 2^24)
+    // top 2^(30 - 54 - lz): exponent -1 - lz, significand top
+    const float h = __int_as_float((int)(((ag_u32)(126 - lz) << 23) | (top & 0x7fffffu) | sgn));
+    // bits 29..7 as an exact float, weight 2^(7 - 54 - lz)
+    const float r = __fsub_rn(__int_as_float((int)(0x4B000000u | ((nl >> 7) & 0x7fffffu))), 8388608.0f);
+    const float l = __fmul_rn(r, __int_as_float((int)(((ag_u32)(80 - lz) << 23) | sgn)));
     return mk(h, l);
 }
 
@@ -90,9 +98,13 @@ __device__ __forceinline__ df normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     const ag_u32 vh = (ag_u32)(V >> 32), vl = (ag_u32)V;
     const ag_u32 K = (vh + 256u) >> 9;   // (V + 2^40) >> 41
     const ag_u32 rh = vh - (K << 9);   // R = rh 2^32 + vl, rh in [-256, 255] as a signed word
-    // R = Rh 2^17 + Rl with Rh = floor(R / 2^17) (|Rh| <= 2^23) and 0 <= Rl < 2^17
-    const int Rh = (int)((rh << 15) | (vl >> 17));
-    const df t = fast_two_sum(__fmul_rn((float)Rh, p2f(-36)), __fmul_rn((float)(vl & 0x1ffffu), p2f(-53)));
+    // R = Rh 2^18 + Rl with Rh = floor(R / 2^18) (|Rh| <= 2^22) and 0 <= Rl < 2^18,
+    // both made exact floats by exponent tricks (no conversion unit): Rh as
+    // (1.5 2^23 + Rh) - 1.5 2^23, Rl as (2^23 + Rl) - 2^23
+    const int Rh = (int)((rh << 14) | (vl >> 18));
+    const float fh = __fsub_rn(__int_as_float(0x4B400000 + Rh), 12582912.0f);
+    const float fl = __fsub_rn(__int_as_float((int)(0x4B000000u | (vl & 0x3ffffu))), 8388608.0f);
+    const df t = fast_two_sum(__fmul_rn(fh, p2f(-35)), __fmul_rn(fl, p2f(-53)));
     const df sn = sin_from_period_table(ld4(kSinCosPiPeriod, (int)K), t);
     return U ? mul_u(sv, sn) : mul(sv, sn);
 }
