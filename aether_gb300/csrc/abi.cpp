@@ -570,9 +570,11 @@ AG_EXPORT int aether_batch_create(void* const* plans, int n_plans, const AetherL
         if (B->block % 32 || B->block < 32 || B->block > 1024)
             throw std::runtime_error("batch_create: block must be a multiple of 32 in [32, 1024]");
         if (B->ipt < 1 || B->ipt > 8) throw std::runtime_error("batch_create: ipt must be in [1, 8]");
+        const int min_blocks = lowering && lowering->min_blocks > 0 ? lowering->min_blocks : 0;
+        if (min_blocks > 32) throw std::runtime_error("batch_create: min_blocks above 32");
         std::vector<const ag::Plan*> ps;
         std::vector<ag::Lowering> lows;
-        std::string key = std::to_string(B->block) + "/" + std::to_string(B->ipt);
+        std::string key = std::to_string(B->block) + "/" + std::to_string(B->ipt) + "/" + std::to_string(min_blocks);
         for (int p = 0; p < n_plans; ++p) {
             PlanObj* P = static_cast<PlanObj*>(plans[p]);
             if (!P) throw std::runtime_error("batch_create: null plan");
@@ -589,7 +591,7 @@ AG_EXPORT int aether_batch_create(void* const* plans, int n_plans, const AetherL
         char nm[40];
         std::snprintf(nm, sizeof nm, "ag_batch_%08x", unsigned(ag::fnv1a(key) & 0xffffffffu));
         B->name = nm;
-        B->source = ag::generate_batch_source(ps, lows, B->block, B->ipt, B->name);
+        B->source = ag::generate_batch_source(ps, lows, B->block, B->ipt, B->name, min_blocks);
         ck(cudaFree(nullptr), "CUDA context");
         B->compiled = ag::compile_cached(B->source, "batch");
         ck(cudaLibraryLoadData(&B->library, B->compiled.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),

@@ -1212,7 +1212,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
 namespace ag {
 
 std::string generate_batch_source(const std::vector<const Plan*>& plans, const std::vector<Lowering>& lows,
-                                  int block, int ipt, const std::string& base) {
+                                  int block, int ipt, const std::string& base, int min_blocks) {
     std::ostringstream o;
     bool emu = false;
     for (const Lowering& l : lows) emu = emu || l.math >= 1;
@@ -1235,7 +1235,8 @@ std::string generate_batch_source(const std::vector<const Plan*>& plans, const s
     // The work list: one argument block per item, the first global tile of the
     // item, and the plan it runs. Items are sorted by tile0.
     o << "struct AgItem {\n    AgArgs a;\n    ag_u64 tile0;\n    int plan;\n    int pad;\n};\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(AG_BLOCK) " << base
+    o << "extern \"C\" __global__ void __launch_bounds__(AG_BLOCK"
+      << (min_blocks > 0 ? ", " + std::to_string(min_blocks) : std::string()) << ") " << base
       << "(const AgItem* __restrict__ items, int n_items, ag_u64 total_tiles) {\n";
     o << "    __shared__ int s_item;\n";
     o << "    for (ag_u64 t = blockIdx.x; t < total_tiles; t += gridDim.x) {\n";

@@ -76,7 +76,8 @@ std::string generate_source(const Plan& plan, const Lowering& low, const std::st
 // block*ipt*vec_p samples that CTAs take round-robin. All plans share block
 // and ipt; each keeps its own math mode and vector width.
 std::string generate_batch_source(const std::vector<const Plan*>& plans, const std::vector<Lowering>& lows,
-                                  int block, int ipt, const std::string& base);
+                                  int block, int ipt, const std::string& base,
+                                  int min_blocks = 0);
 
 // Kernel base name of a plan: ag_<expr|fill|sum>_<8 hex digits of the text hash>,
 // so profiles and launch lists tell plans apart.

@@ -825,8 +825,15 @@ AG_EXPORT int aether_serve_open(void* const* plans, int n_plans, const AetherSer
         if (S->cfg.grouping != 0 && S->cfg.grouping != 1) throw std::runtime_error("serve_open: grouping must be 0 or 1");
         if (S->cfg.mode == AETHER_SERVE_BATCHED && S->cfg.grouping == 0) {
             for (int p = 0; p < n_plans; ++p) {
+                // each plan's work-list kernel takes the plan's own block shape
+                // and occupancy bound (its tuned lowering) unless the server sets one
+                const PlanObj* P = S->plans[size_t(p)];
+                AetherLowering lp{};
+                lp.block = config->block > 0 ? config->block : P->low.block;
+                lp.ipt = config->ipt > 0 ? config->ipt : P->low.ipt;
+                lp.min_blocks = config->block > 0 ? 0 : P->low.min_blocks;
                 void* b = nullptr;
-                if (aether_batch_create(&plans[p], 1, &low, &b) != AETHER_OK)
+                if (aether_batch_create(&plans[p], 1, &lp, &b) != AETHER_OK)
                     throw std::runtime_error(aether_last_error());
                 S->plan_batch.push_back(static_cast<BatchObj*>(b));
             }

@@ -54,8 +54,20 @@ class ShapeTemplate:
         self.order = [int(ptr) - 1 for (ptr, _p, _d, _c, _o) in ctx.operands]
         self.scalars = list(ctx.scalars)
         self.keys = list(ctx.keys)
-        self.plan = get_plan(self.ir, math=math, contract=contract)
+        self.build = build
+        self.math, self.contract = math, contract
+        self.plan = get_plan(self.ir, math=math, contract=contract, **self._tuned())
         self.out_comps = int(np.prod(self.out_shape)) if self.out_shape else 1
+
+    def _tuned(self):
+        """The autotuned lowering of this shape's plan on this device, if any
+        (aether_gb300.tune; tune_standard_shapes measures them)."""
+        try:
+            from . import tune
+            low = tune.tuned(self.ir, self.math, self.contract)
+        except Exception:   # no device to key the cache on
+            low = None
+        return dict(low) if low else {}
 
     def operand_bytes(self, k, n):
         dt, sh = self.operands[k]
@@ -95,6 +107,34 @@ def standard_shapes():
         ShapeTemplate("quatrot_f64", "f64", v3, [("f64", v4), ("f64", v3)], lambda q, v: q.quatRotate(v), math=1),
         ShapeTemplate("inv3_f64", "f64", m9, [("f64", m9)], inv, math=1),
     ]
+
+
+def tune_standard_shapes(n=1 << 21, shapes=None, verbose=False):
+    """Autotune the plan of every served shape on device arrays of n samples
+    (uniform values in [-1, 1)) and cache the winners (aether_gb300.tune).
+    Shapes built afterwards take the tuned lowering, and so do the serving
+    loop's per-plan work-list kernels."""
+    import aether_gb300 as ag
+    from . import tune
+    shapes = shapes or standard_shapes()
+    results = {}
+    for k, sh in enumerate(shapes):
+        arrays = []
+        for j, (dt, shape) in enumerate(sh.operands):
+            a = ag.Array(dt, shape, n)
+            comps = int(np.prod(shape)) if shape else 1
+            ag.assign(a, ag.Generator(1000 + k).substream(j).uniform(comps, -1.0, 1.0).reshape(shape)
+                      if len(shape) > 1 else ag.Generator(1000 + k).substream(j).uniform(comps, -1.0, 1.0))
+            arrays.append(a)
+        dst = ag.Array(sh.out_dtype, sh.out_shape, n)
+        expr = sh.build(*[a.view() for a in arrays])
+
+        def make(**low):
+            return ag.prepare(dst, expr, math=sh.math, contract=sh.contract, **low)
+
+        best, res = tune.tune(make, sh.ir, sh.math, sh.contract, verbose=verbose)
+        results[sh.name] = (best, res[0][0] if res else None)
+    return results
 
 
 class HostPools:
