@@ -133,6 +133,73 @@ int main(int argc, char** argv) {
         dumpArray("leaf_bernoulli", be);
         dumpArray("leaf_uniform_item", ui);
     }
+    // The rest of the leaf API, read per sample with get<I>(i) as the
+    // reference's random tests do: per-component (Item) parameters of every
+    // distribution, uniformInt, multivariateNormal from cholesky, the
+    // index-free get<I>() draws and the free-function spelling.
+    {
+        const std::size_t n = 1000;
+        Generator g(21);
+        aether::Item<double, 3> m3, s3, l3, p3;
+        m3(0) = -1.0; m3(1) = 0.0; m3(2) = 2.5;
+        s3(0) = 0.5; s3(1) = 1.0; s3(2) = 3.0;
+        l3(0) = 0.5; l3(1) = 2.0; l3(2) = 8.0;
+        p3(0) = 0.1; p3(1) = 0.5; p3(2) = 0.9;
+        const auto nrm = g.substream(0).normal<double, 3>(m3, s3);
+        const auto lgn = g.substream(1).lognormal<double, 3>(m3, s3);
+        const auto ex = g.substream(2).exponential<double, 3>(l3);
+        const auto be = g.substream(3).bernoulli<double, 3>(p3);
+        const auto ri = g.substream(4).uniformInt<int, 3>(-5, 17);
+        const auto rl = g.substream(5).uniformInt<long long, 2>(-(1LL << 40), 1LL << 41);
+        const double cov[3][3] = {{2.0, 0.5, 0.1}, {0.5, 1.0, 0.3}, {0.1, 0.3, 0.5}};
+        const auto L = aether::random::cholesky<double, 3>(cov);
+        aether::Item<double, 3> mu;
+        mu(0) = 1.0; mu(1) = -2.0; mu(2) = 0.5;
+        const auto mvn = g.substream(6).multivariateNormal<double, 3>(mu, L);
+        const float covf[2][2] = {{1.5f, -0.4f}, {-0.4f, 0.8f}};
+        const auto Lf = aether::random::cholesky<float, 2>(covf);
+        aether::Item<float, 2> muf;
+        muf(0) = 0.25f; muf(1) = -0.75f;
+        const auto mvnf = g.substream(7).multivariateNormal<float, 2>(muf, Lf);
+        const auto fu = aether::random::uniform<double, 2>(-3.0, 3.0);
+        const auto fs = aether::random::seed(99).normal<double, 2>(0.0, 1.0);
+        std::vector<double> vn(3 * n), vl(3 * n), ve(3 * n), vb(3 * n), vm(3 * n), vfu(2 * n), vfs(2 * n);
+        std::vector<int> vi(3 * n);
+        std::vector<long long> vll(2 * n);
+        std::vector<float> vmf(2 * n);
+        for (std::size_t k = 0; k < n; ++k) {
+            const SampleIndex i = SampleIndex::make(k);
+            vn[k] = nrm.get<0>(i); vn[n + k] = nrm.get<1>(i); vn[2 * n + k] = nrm.get<2>(i);
+            vl[k] = lgn.get<0>(i); vl[n + k] = lgn.get<1>(i); vl[2 * n + k] = lgn.get<2>(i);
+            ve[k] = ex.get<0>(i); ve[n + k] = ex.get<1>(i); ve[2 * n + k] = ex.get<2>(i);
+            vb[k] = be.get<0>(i); vb[n + k] = be.get<1>(i); vb[2 * n + k] = be.get<2>(i);
+            vi[k] = ri.get<0>(i); vi[n + k] = ri.get<1>(i); vi[2 * n + k] = ri.get<2>(i);
+            vll[k] = rl.get<0>(i); vll[n + k] = rl.get<1>(i);
+            vm[k] = mvn.get<0>(i); vm[n + k] = mvn.get<1>(i); vm[2 * n + k] = mvn.get<2>(i);
+            vmf[k] = mvnf.get<0>(i); vmf[n + k] = mvnf.get<1>(i);
+            vfu[k] = fu.get<0>(i); vfu[n + k] = fu.get<1>(i);
+            vfs[k] = fs.get<0>(i); vfs[n + k] = fs.get<1>(i);
+        }
+        dump<double>("leafi_normal", vn.data(), 3, n, n, "f64");
+        dump<double>("leafi_lognormal", vl.data(), 3, n, n, "f64");
+        dump<double>("leafi_exponential", ve.data(), 3, n, n, "f64");
+        dump<double>("leafi_bernoulli", vb.data(), 3, n, n, "f64");
+        dump<int>("leaf_uniform_int", vi.data(), 3, n, n, "i32");
+        dump<long long>("leaf_uniform_int64", vll.data(), 2, n, n, "i64");
+        dump<double>("leaf_mvn", vm.data(), 3, n, n, "f64");
+        dump<float>("leaf_mvn_f32", vmf.data(), 2, n, n, "f32");
+        dump<double>("free_uniform", vfu.data(), 2, n, n, "f64");
+        dump<double>("free_seed_normal", vfs.data(), 2, n, n, "f64");
+        dump<double>("mvn_cholesky", L.data, 1, 6, 6, "f64");
+        // index-free draws: one value per component, the same at every sample
+        const auto u = g.substream(8).uniform<double, 3>(-1.0, 1.0);
+        const auto z = g.substream(9).normal<float, 2>(0.0f, 1.0f);
+        const double fr[] = {u.get<0>(), u.get<1>(), u.get<2>(), double(z.get<0>()), double(z.get<1>()),
+                             nrm.get<2>(), lgn.get<0>(), ex.get<1>(), be.get<2>(), double(ri.get<0>()),
+                             double(ri.get<2>()), double(rl.get<1>()), mvn.get<0>(), mvn.get<2>(),
+                             double(mvnf.get<1>()), fu.get<1>()};
+        dump<double>("index_free", fr, 1, sizeof(fr) / sizeof(*fr), sizeof(fr) / sizeof(*fr), "f64");
+    }
     // Geometry (config 4 node kinds) on uniform(-1,1) inputs, Generator(5).
     {
         const std::size_t n = 777;

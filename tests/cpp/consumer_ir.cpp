@@ -32,6 +32,12 @@ int main() {
     emit("uniform", a, g.substream(0).uniform<double, 3>(-1.0, 1.0));
     auto z = fake<double>(0x60000, n);
     emit("normal", z, random::Generator(7).substream(4).normal<double, 1>(0.0, 1.0));
+    Item<double, 3> m3, s3, l3;
+    m3(0) = -1.0; m3(1) = 0.0; m3(2) = 2.5;
+    s3(0) = 0.5; s3(1) = 1.0; s3(2) = 3.0;
+    l3(0) = 0.5; l3(1) = 2.0; l3(2) = 8.0;
+    emit("normal_item", a, random::Generator(21).substream(0).normal<double, 3>(m3, s3));
+    emit("exponential_item", a, random::Generator(21).substream(2).exponential<double, 3>(l3));
     auto q = fake<double, 4>(0x70000, n);
     auto m = fake<double, 3, 3>(0x80000, n), mi = fake<double, 3, 3>(0x90000, n);
     emit("cross", d, a.cross(b));

@@ -67,7 +67,7 @@ def run_reference(ref):
         manifest = json.loads(subprocess.check_output([exe, d]))
         arrays = {}
         for m in manifest:
-            dt = np.float64 if m["dtype"] == "f64" else np.float32
+            dt = {"f64": np.float64, "f32": np.float32, "i32": np.int32, "i64": np.int64}[m["dtype"]]
             a = np.fromfile(os.path.join(d, m["name"] + ".bin"), dtype=dt)
             arrays[m["name"]] = a.reshape(m["comps"], m["n"])
     return arrays

@@ -42,6 +42,11 @@ def _python_texts():
          E.cwiseRsqrt(E.constant(1.0, (3,)) + d0 * d0))
     emit("uniform", "f64", (3,), Generator(42).substream(0).uniform(3, -1.0, 1.0))
     emit("normal", "f64", (1,), Generator(7).substream(4).normal(1, 0.0, 1.0))
+    m3 = E.stack(*(E.Scalar(v) for v in (-1.0, 0.0, 2.5)))
+    s3 = E.stack(*(E.Scalar(v) for v in (0.5, 1.0, 3.0)))
+    l3 = E.stack(*(E.Scalar(v) for v in (0.5, 2.0, 8.0)))
+    emit("normal_item", "f64", (3,), Generator(21).substream(0).normal(3, m3, s3))
+    emit("exponential_item", "f64", (3,), Generator(21).substream(2).exponential(3, l3))
     q = Operand(0x70000, n, "f64", (4,))
     m = Operand(0x80000, n, "f64", (3, 3))
     emit("cross", "f64", (3,), a.cross(b))

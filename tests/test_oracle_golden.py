@@ -115,6 +115,26 @@ def test_uniform_item_parameters(oracle, ref_cases):
     assert np.array_equal(d, ref_cases["leaf_uniform_item"])
 
 
+ITEM_LEAVES = {
+    # (substream, IR, scalars): per-component parameters as stacked scalars,
+    # the Items of the reference driver's Generator(21) cases
+    "leafi_normal": (0, "(plan f64 [3] set (normal 0 (stack (sc 0) (sc 1) (sc 2)) (stack (sc 3) (sc 4) (sc 5)) 3))",
+                     [-1.0, 0.0, 2.5, 0.5, 1.0, 3.0]),
+    "leafi_lognormal": (1, "(plan f64 [3] set (lognormal 0 (stack (sc 0) (sc 1) (sc 2)) "
+                           "(stack (sc 3) (sc 4) (sc 5)) 3))", [-1.0, 0.0, 2.5, 0.5, 1.0, 3.0]),
+    "leafi_exponential": (2, "(plan f64 [3] set (exponential 0 (stack (sc 0) (sc 1) (sc 2)) 3))", [0.5, 2.0, 8.0]),
+    "leafi_bernoulli": (3, "(plan f64 [3] set (bernoulli 0 (stack (sc 0) (sc 1) (sc 2)) 3))", [0.1, 0.5, 0.9]),
+}
+
+
+@pytest.mark.parametrize("name", sorted(ITEM_LEAVES))
+def test_item_parameter_leaves_match_reference(oracle, ref_cases, name):
+    sub, ir, scalars = ITEM_LEAVES[name]
+    key = oracle.substream_key(oracle.generator_key(21), sub)
+    d, _ = oracle.eval_ir(ir, 1000, [], scalars=scalars, keys=[key], dst_comps=3)
+    assert ulp_diff(d, ref_cases[name]).max() <= 1
+
+
 GEO = {
     "geo_cross": ("(plan f64 [3] set (cross (in 0 f64 [3]) (in 1 f64 [3])))", ["geo_a", "geo_b"], 3),
     "geo_qrot": ("(plan f64 [3] set (qrot (in 0 f64 [4]) (in 1 f64 [3])))", ["geo_q", "geo_a"], 3),

@@ -377,6 +377,28 @@ def test_uniform_item_parameters(ref_cases):
     assert np.array_equal(d.host(), ref_cases["leaf_uniform_item"])
 
 
+@pytest.mark.parametrize("name", ["leafi_normal", "leafi_lognormal", "leafi_exponential", "leafi_bernoulli"])
+def test_item_parameter_leaves(ref_cases, name):
+    """Per-component (Item) parameters of every distribution through the
+    engine's whole-view kernel, against the reference driver's Generator(21)
+    draws: bernoulli bit-exact, the rest within the reference's 1e-12."""
+    def item(*v):
+        return ag.stack(*(ag.expr.Scalar(x) for x in v))
+    m3, s3 = item(-1.0, 0.0, 2.5), item(0.5, 1.0, 3.0)
+    g = ag.Generator(21)
+    leaf = {"leafi_normal": lambda: g.substream(0).normal(3, m3, s3),
+            "leafi_lognormal": lambda: g.substream(1).lognormal(3, m3, s3),
+            "leafi_exponential": lambda: g.substream(2).exponential(3, item(0.5, 2.0, 8.0)),
+            "leafi_bernoulli": lambda: g.substream(3).bernoulli(3, item(0.1, 0.5, 0.9))}[name]()
+    d = ag.Array("f64", (3,), 1000)
+    ag.assign(d, leaf, contract=0)
+    ref = ref_cases[name]
+    if name == "leafi_bernoulli":
+        assert np.array_equal(d.host(), ref)
+    else:
+        assert np.all(np.abs(d.host() - ref) <= 1e-12 * (1 + np.abs(ref))), name
+
+
 # ---------------------------------------------------------------------------
 # Interpreter-checked cases (arbitrary trees against the oracle)
 # ---------------------------------------------------------------------------
