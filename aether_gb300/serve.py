@@ -64,7 +64,7 @@ class ShapeTemplate:
         (aether_gb300.tune; tune_standard_shapes measures them)."""
         try:
             from . import tune
-            low = tune.tuned(self.ir, self.math, self.contract)
+            low = tune.tuned(self.ir, self.math, self.contract, regime="serve")
         except Exception:   # no device to key the cache on
             low = None
         return dict(low) if low else {}
@@ -111,7 +111,8 @@ def standard_shapes():
 
 def tune_standard_shapes(n=1 << 21, shapes=None, verbose=False):
     """Autotune the plan of every served shape on device arrays of n samples
-    (uniform values in [-1, 1)) and cache the winners (aether_gb300.tune).
+    (uniform values in [-1, 1)) and cache the winners under the "serve" regime
+    (aether_gb300.tune).
     Shapes built afterwards take the tuned lowering, and so do the serving
     loop's per-plan work-list kernels."""
     import aether_gb300 as ag
@@ -132,7 +133,7 @@ def tune_standard_shapes(n=1 << 21, shapes=None, verbose=False):
         def make(**low):
             return ag.prepare(dst, expr, math=sh.math, contract=sh.contract, **low)
 
-        best, res = tune.tune(make, sh.ir, sh.math, sh.contract, verbose=verbose)
+        best, res = tune.tune(make, sh.ir, sh.math, sh.contract, verbose=verbose, regime="serve")
         results[sh.name] = (best, res[0][0] if res else None)
     return results
 

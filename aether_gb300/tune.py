@@ -67,10 +67,19 @@ def _generated_digest(ir, math, contract):
     return hashlib.sha1(src.encode()).hexdigest()[:16]
 
 
-def _key(ir, math, contract):
+def _key(ir, math, contract, regime=""):
+    """The cache key of a plan's tuning. `regime` names the launch sizes it was
+    measured at: "" for whole-array launches (the benchmarks' 2^26..2^28
+    samples), "serve" for served requests (2^21 samples), whose winners differ
+    (tail effects favour smaller blocks)."""
     h = hashlib.sha1(("%s|%d|%d|%s|%s|%s" % (ir, math, contract, _device_name(), _code_digest(),
                                              _generated_digest(ir, math, contract))).encode()).hexdigest()
-    return h
+    return regime_key(h, regime)
+
+
+def regime_key(key, regime):
+    """The key of `regime`'s entry from the whole-array key of the same plan."""
+    return key if not regime else hashlib.sha1(("%s|%s" % (key, regime)).encode()).hexdigest()
 
 
 SHIPPED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned.json")
@@ -106,13 +115,13 @@ def store(key, rec):
         os.replace(tmp, path)
 
 
-def tuned(ir, math=0, contract=-1):
+def tuned(ir, math=0, contract=-1, regime=""):
     """The cached winning lowering for a plan, or None."""
-    rec = load().get(_key(ir, math, contract))
+    rec = load().get(_key(ir, math, contract, regime))
     return rec["lowering"] if rec else None
 
 
-def tune(make_launch, ir, math=0, contract=-1, candidates=None, reps=5, warmup=2, verbose=False):
+def tune(make_launch, ir, math=0, contract=-1, candidates=None, reps=5, warmup=2, verbose=False, regime=""):
     """Time `make_launch(**lowering)` for each candidate lowering and cache the
     fastest. `make_launch` returns a callable that enqueues one evaluation on
     the current stream (aether_gb300.prepare(...)). Returns (best, results)."""
@@ -142,6 +151,6 @@ def tune(make_launch, ir, math=0, contract=-1, candidates=None, reps=5, warmup=2
         raise RuntimeError("autotune: no candidate lowering ran")
     results.sort(key=lambda r: r[0])
     best = results[0]
-    store(_key(ir, math, contract), {"lowering": best[1], "ms": best[0], "registers": best[2],
+    store(_key(ir, math, contract, regime), {"lowering": best[1], "ms": best[0], "registers": best[2],
                                       "blocks_per_sm": best[3], "candidates": len(results)})
     return best[1], results

@@ -56,3 +56,17 @@ def test_shipped_table_under_the_user_cache(cache, monkeypatch, tmp_path):
     assert tune.tuned(ir, 1)["block"] == 128               # shipped entry
     tune.store(key, {"lowering": {"block": 512, "ipt": 2, "vec": 0, "min_blocks": 0}})
     assert tune.tuned(ir, 1)["block"] == 512               # the user cache wins
+
+
+def test_regimes_keep_separate_winners(cache):
+    """A plan's serving winner (2^21-sample requests) and its whole-array
+    winner are separate entries; the whole-array key is the regime-free one."""
+    ir = _ir(lambda a: a * 3.0)
+    assert tune._key(ir, 1, -1, "") == tune._key(ir, 1, -1)
+    assert tune._key(ir, 1, -1, "serve") == tune.regime_key(tune._key(ir, 1, -1), "serve")
+    assert tune._key(ir, 1, -1, "serve") != tune._key(ir, 1, -1)
+    tune.store(tune._key(ir, 1, -1), {"lowering": {"block": 512, "ipt": 1, "vec": 0, "min_blocks": 0}})
+    assert tune.tuned(ir, 1, regime="serve") is None
+    tune.store(tune._key(ir, 1, -1, "serve"), {"lowering": {"block": 128, "ipt": 2, "vec": 1, "min_blocks": 0}})
+    assert tune.tuned(ir, 1)["block"] == 512
+    assert tune.tuned(ir, 1, regime="serve")["block"] == 128
