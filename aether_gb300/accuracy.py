@@ -35,6 +35,16 @@ EMU_EXPR_BOUND_2M53 = 512
 # Emulated Box-Muller normals, abs+rel (measured 194 x 2^-53 over 2^25 draws).
 EMU_NORMAL_BOUND_2M53 = 256
 
+# FP64-grade lowering (math 3): doubles split exactly into three floats; sums,
+# products, quotients, sqrt, rsqrt, log and log1p in triple-float arithmetic
+# (each within about 2^-60 relative on the host check against 113-bit
+# arithmetic, tests/emu_host/tf_check.cpp), exp and trig on the native pipe;
+# each output is the triple-float value rounded once to a double. Against
+# exact arithmetic: this many ulps of the term scale (measured 1.0 on the
+# host, the final rounding). Against the oracle (itself a few ulps from exact)
+# the native bound NATIVE_EXPR_ULPS applies.
+FP64_GRADE_EXACT_ULPS = 2
+
 # Precision form (math 2): float-float outputs and the FP64-finished global
 # sum, relative to FP64 evaluation of the same f32 inputs.
 PRECISION_FF_REL = 1e-12

@@ -331,7 +331,9 @@ AG_EXPORT int aether_plan_create(const char* ir, const AetherLowering* lowering,
             throw std::runtime_error("plan_create: the precision form (math = 2) applies to f32 and ff plans");
         if (P->plan.dst_dtype == ag::DType::FF && P->low.math != 2)
             throw std::runtime_error("plan_create: ff destinations are written by the precision form (math = 2)");
-        if (P->low.math < 0 || P->low.math > 2) throw std::runtime_error("plan_create: math must be 0, 1 or 2");
+        if (P->low.math == 3 && P->plan.dst_dtype != ag::DType::F64)
+            throw std::runtime_error("plan_create: FP64-grade triple-float (math = 3) applies to f64 plans");
+        if (P->low.math < 0 || P->low.math > 3) throw std::runtime_error("plan_create: math must be 0, 1, 2 or 3");
         P->name = ag::kernel_base(P->plan, ir);
         P->source = ag::generate_source(P->plan, P->low, P->name);
         ck(cudaFree(nullptr), "CUDA context");   // make the primary context current

@@ -405,13 +405,16 @@ struct Gen {
     std::ostringstream pro;   // sample-0 prologue (at0 subtrees)
     std::ostringstream body;  // per-lane code
     bool dfm = false;         // double-float working type (emulated FP64)
+    bool tfm = false;         // with dfm: triple-float working type (FP64-grade, math 3)
+    std::string NS = "ag::e64::";   // namespace of the working type's functions
     std::string pre = "t";    // variable prefix
     bool direct = false;      // leaves load their own sample `s` (per-lane fallback function)
     std::vector<signed char> nn_memo;
     // Double-float magnitude bounds: floor(log2 |v|) of every non-zero value of
     // node id lies in [elo, ehi] (wide open when unknown). A product whose
     // bounds cannot go below 2^-102 needs no range check (ag::e64::ck).
-    static constexpr int kOpenLo = -100000, kOpenHi = 100000, kSafeLo = -101;
+    static constexpr int kOpenLo = -100000, kOpenHi = 100000;
+    int kSafeLo = -101;   // products at or above 2^kSafeLo need no check (-80 for triple-float)
     std::vector<int> elo, ehi;
     std::string cur_ok = "ok_";   // the range flag of the node being emitted
 
@@ -438,9 +441,12 @@ struct Gen {
     }
 
     Gen(const Plan& p, const Lowering& l, const std::vector<int>& c, bool df_mode = false, std::string prefix = "t",
-        bool force_double = false)
-        : P(p), L(l), ctx(c), val(p.nodes.size()), done(p.nodes.size(), 0), dfm(df_mode), pre(std::move(prefix)) {
-        W = dfm ? "ag::e64::df" : ((P.dst_dtype == DType::F64 || force_double) ? "double" : "float");
+        bool force_double = false, bool tf_mode = false)
+        : P(p), L(l), ctx(c), val(p.nodes.size()), done(p.nodes.size(), 0), dfm(df_mode || tf_mode), tfm(tf_mode),
+          pre(std::move(prefix)) {
+        NS = tfm ? "ag::t64::" : "ag::e64::";
+        if (tfm) kSafeLo = -80;
+        W = tfm ? "ag::t64::tf" : dfm ? "ag::e64::df" : ((P.dst_dtype == DType::F64 || force_double) ? "double" : "float");
         S = P.dst_dtype == DType::F64 ? "double" : "float";
     }
 
@@ -448,23 +454,23 @@ struct Gen {
     // of two of them are exact two-products, no double-float multiply.
     bool exact_f32(int id) const {
         const Node& n = P.nodes[size_t(id)];
-        return dfm && n.op == "in" && n.dtype == DType::F32;
+        return dfm && !tfm && n.op == "in" && n.dtype == DType::F32;
     }
     // `u`: the product is read only by sums and may stay unnormalised. The
     // range check is left out when the factors' bounds keep it above 2^-102.
     std::string mulx(bool u, int ia, int ib, const std::string& a, const std::string& b) {
         const bool safe = lo_of(ia) + lo_of(ib) >= kSafeLo;
         if (exact_f32(ia) && exact_f32(ib)) {
-            const std::string p = "ag::e64::two_prod(" + a + ".hi, " + b + ".hi)";
+            const std::string p = NS + "two_prod(" + a + ".hi, " + b + ".hi)";
             return checked(p, safe);
         }
         if (dfm && ia == ib && a == b) return checked(sqr(u, a), safe);   // x*x: the square's cheaper form
-        return dfm ? checked("ag::e64::mul(" + a + ", " + b + ")", safe) : mul(a, b);
+        return dfm ? checked(NS + "mul(" + a + ", " + b + ")", safe) : mul(a, b);
     }
     int lo_of(int id) const { return elo.empty() ? kOpenLo : elo[size_t(id)]; }
     int hi_of(int id) const { return ehi.empty() ? kOpenHi : ehi[size_t(id)]; }
     std::string checked(const std::string& v, bool safe) const {
-        return safe ? v : "ag::e64::ck(" + v + ", " + cur_ok + ")";
+        return safe ? v : NS + "ck(" + v + ", " + cur_ok + ")";
     }
     // Nodes read only by sums (add, sub): a square feeding them may stay an
     // unnormalised pair, saving its final Fast2Sum. The root of an emulated
@@ -482,14 +488,14 @@ struct Gen {
         }
         return sum_only_memo[size_t(id)] != 0;
     }
-    std::string sqr(bool u, const std::string& x) { return (u ? "ag::e64::sqr_u(" : "ag::e64::sqr(") + x + ")"; }
+    std::string sqr(bool u, const std::string& x) { return (u ? NS + "sqr_u(" : NS + "sqr(") + x + ")"; }
 
     std::string add(const std::string& a, const std::string& b) const {
-        if (dfm) return "ag::e64::add(" + a + ", " + b + ")";
+        if (dfm) return NS + "add(" + a + ", " + b + ")";
         return L.contract ? "(" + a + " + " + b + ")" : "ag::rn_add(" + a + ", " + b + ")";
     }
     std::string sub(const std::string& a, const std::string& b) const {
-        if (dfm) return "ag::e64::sub(" + a + ", " + b + ")";
+        if (dfm) return NS + "sub(" + a + ", " + b + ")";
         return L.contract ? "(" + a + " - " + b + ")" : "ag::rn_sub(" + a + ", " + b + ")";
     }
     // Products and quotients inside composite nodes carry the range check
@@ -499,22 +505,37 @@ struct Gen {
     // the kids' bounds keep every such product above 2^-102.
     bool kids_safe = false;
     std::string mulkk(const std::string& a, const std::string& b) const {
-        if (dfm && kids_safe) return "ag::e64::mul(" + a + ", " + b + ")";
+        if (dfm && kids_safe) return NS + "mul(" + a + ", " + b + ")";
         return mul(a, b);
     }
     std::string mul(const std::string& a, const std::string& b) const {
-        if (dfm && (zero_vars.count(a) || zero_vars.count(b))) return "ag::e64::mul(" + a + ", " + b + ")";
-        if (dfm) return "ag::e64::ck(ag::e64::mul(" + a + ", " + b + "), " + cur_ok + ")";
+        if (dfm && (zero_vars.count(a) || zero_vars.count(b))) return NS + "mul(" + a + ", " + b + ")";
+        if (dfm) return NS + "ck(" + NS + "mul(" + a + ", " + b + "), " + cur_ok + ")";
         return L.contract ? "(" + a + " * " + b + ")" : "ag::rn_mul(" + a + ", " + b + ")";
     }
     std::string div(const std::string& a, const std::string& b) const {
-        if (dfm) return "ag::e64::ck(ag::e64::div(" + a + ", " + b + "), " + cur_ok + ")";
+        if (dfm) return NS + "ck(" + NS + "div(" + a + ", " + b + "), " + cur_ok + ")";
         return "ag::rn_div(" + a + ", " + b + ")";
     }
-    std::string neg(const std::string& a) const { return dfm ? "ag::e64::neg(" + a + ")" : "(-" + a + ")"; }
+    std::string neg(const std::string& a) const { return dfm ? NS + "neg(" + a + ")" : "(-" + a + ")"; }
     std::string lit(double v) const {
-        if (dfm) return "ag::e64::dfc(" + hexlit(v) + ")";
+        if (tfm) return tf_literal(v);
+        if (dfm) return NS + "dfc(" + hexlit(v) + ")";
         return "((" + W + ")" + hexlit(v) + ")";
+    }
+    // A literal as three floats split here, exactly for every normal double
+    // (no FP64 work in the kernel).
+    static std::string fltlit(float f) {
+        char b[48];
+        std::snprintf(b, sizeof b, "%.9ef", double(f));
+        return std::isfinite(f) ? std::string(b) : (f != f ? "__int_as_float(0x7fc00000)" : (f > 0 ? "__int_as_float(0x7f800000)" : "__int_as_float((int)0xff800000)"));
+    }
+    std::string tf_literal(double v) const {
+        const float x = float(v);
+        const double r = std::isfinite(x) ? v - double(x) : 0.0;
+        const float y = float(r);
+        const float z = float(r - double(y));
+        return "ag::t64::mk3(" + fltlit(x) + ", " + fltlit(y) + ", " + fltlit(z) + ")";
     }
     std::string okv(int id) const { return ctx[size_t(id)] ? "ok0_" : "ok_"; }
     // |x| of a loaded operand: non-negative and, once the operand passed the
@@ -529,14 +550,14 @@ struct Gen {
         for (size_t i = 0; i < args.size(); ++i) a += (i ? ", " : "") + args[i];
         if (!dfm) return "ag::f_" + name + "(" + a + ")";
         static const std::set<std::string> own = {"sqrt", "rsqrt", "log", "log1p", "abs", "sign", "min", "max"};
-        if (name == "sin" || name == "cos" || name == "exp") return "ag::e64::" + name + "_(" + a + ", " + okv(id) + ")";
+        if (name == "sin" || name == "cos" || name == "exp") return NS + "" + name + "_(" + a + ", " + okv(id) + ")";
         if (name == "log1p" && abs_of_input(P.nodes[size_t(id)].kids[0]))
-            return "ag::e64::log1p_nn_(" + a + ")";   // |input| is >= 0 and within the input range check
-        if (own.count(name)) return "ag::e64::" + name + "_(" + a + ")";
-        return "ag::e64::nat_" + name + "(" + a + ")";
+            return NS + "log1p_nn_(" + a + ")";   // |input| is >= 0 and within the input range check
+        if (own.count(name)) return NS + "" + name + "_(" + a + ")";
+        return NS + "nat_" + name + "(" + a + ")";
     }
     std::string gtx(const std::string& a, const std::string& b) const {
-        return dfm ? "ag::e64::gt(" + a + ", " + b + ")" : "(" + a + " > " + b + ")";
+        return dfm ? NS + "gt(" + a + ", " + b + ")" : "(" + a + " > " + b + ")";
     }
 
     std::ostringstream& out_for(int id) { return ctx[size_t(id)] ? pro : body; }
@@ -570,7 +591,7 @@ struct Gen {
         auto clampb = [](int v) { return v < kOpenLo ? kOpenLo : (v > kOpenHi ? kOpenHi : v); };
         int lo = kOpenLo, hi = kOpenHi;
         if (op == "in") {
-            if (n.dtype == DType::F64) lo = -50, hi = 60;
+            if (n.dtype == DType::F64) lo = tfm ? -40 : -50, hi = 60;
             else if (n.dtype == DType::F32) lo = -149, hi = 127;
         } else if (op == "lit") {
             if (n.lit != 0.0 && std::isfinite(n.lit)) {
@@ -637,9 +658,10 @@ struct Gen {
                 if (pbool) {
                     e.push_back("(" + src + " != 0)");
                 } else if (dfm && n.dtype == DType::F32) {
-                    e.push_back("ag::e64::mk((float)" + src + ", 0.0f)");   // exact
+                    e.push_back(tfm ? "ag::t64::mk3((float)" + src + ", 0.0f, 0.0f)"
+                                    : NS + "mk((float)" + src + ", 0.0f)");   // exact
                 } else if (dfm) {
-                    e.push_back("ag::e64::from_double_ck((double)" + src + ", " + okv(id) + ")");
+                    e.push_back(NS + "from_double_ck((double)" + src + ", " + okv(id) + ")");
                 } else {
                     e.push_back("(" + W + ")" + src);
                 }
@@ -648,7 +670,7 @@ struct Gen {
         } else if (op == "sc") {
             const std::string s = "a.sc[" + std::to_string(n.k) + "]";
             const std::string k = std::to_string(n.k);
-            def(id, {dfm ? "ag::e64::mk(a.sch[" + k + "], a.scl[" + k + "])" : "(" + W + ")" + s});
+            def(id, {tfm ? "ag::t64::dfc(" + s + ")" : dfm ? NS + "mk(a.sch[" + k + "], a.scl[" + k + "])" : "(" + W + ")" + s});
         } else if (op == "lit") {
             def(id, {lit(n.lit)});
             if (n.lit == 0.0) zero_vars.insert(val[size_t(id)][0]);   // products with it are exact zeros
@@ -663,7 +685,7 @@ struct Gen {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string x = V(0)[size_t(c)];
                 if (op == "sq") e.push_back(dfm ? checked(sqr(sum_only(id), x), 2 * lo_of(n.kids[0]) >= kSafeLo) : mul(x, x));
-                else if (op == "sqrt" && dfm && nonneg(n.kids[0])) e.push_back("ag::e64::sqrt_nn_(" + x + ")");
+                else if (op == "sqrt" && dfm && nonneg(n.kids[0])) e.push_back(NS + "sqrt_nn_(" + x + ")");
                 else if (op == "neg") e.push_back(neg(x));
                 else e.push_back(call(op, {x}, id));
             }
@@ -672,7 +694,7 @@ struct Gen {
             for (int c = 0; c < n.comps; ++c) {
                 const std::string a = V(0)[size_t(c)], b = V(1)[size_t(c)];
                 if (op == "add" && dfm && nonneg(n.kids[0]) && nonneg(n.kids[1]))
-                    e.push_back((root_to_double && id == P.root ? "ag::e64::add_fast_u(" : "ag::e64::add_fast(") + a +
+                    e.push_back((root_to_double && id == P.root ? NS + "add_fast_u(" : NS + "add_fast(") + a +
                                 ", " + b + ")");
                 else if (op == "add") e.push_back(add(a, b));
                 else if (op == "sub") e.push_back(sub(a, b));
@@ -699,7 +721,7 @@ struct Gen {
             const bool logical = op == "and" || op == "or";
             for (int c = 0; c < n.comps; ++c) {
                 const std::string a = V(0)[size_t(c)], b = V(1)[size_t(c)];
-                if (dfm && !logical && !K(0).is_bool) e.push_back("ag::e64::" + op + "(" + a + ", " + b + ")");
+                if (dfm && !logical && !K(0).is_bool) e.push_back(NS + "" + op + "(" + a + ", " + b + ")");
                 else e.push_back("(" + a + " " + sym.at(op) + " " + b + ")");
             }
             def(id, e, true);
@@ -789,7 +811,7 @@ struct Gen {
             auto q = [&](const std::string& num) { return dfm ? mul(num, rd) : div(num, d); };
             if (dim == 2) {
                 o << "        const " << W << " " << d << " = " << sub(mulkk(m[0], m[3]), mulkk(m[1], m[2])) << ";\n";
-                if (dfm && op == "inv") o << "        const " << W << " " << rd << " = ag::e64::recip(" << d << ");\n";
+                if (dfm && op == "inv") o << "        const " << W << " " << rd << " = " << NS << "recip(" << d << ");\n";
                 if (op == "det") e = {d};
                 else e = {q(m[3]), q(neg(m[1])), q(neg(m[2])), q(m[0])};
             } else {
@@ -799,7 +821,7 @@ struct Gen {
                   << add(sub(mul(a, sub(mulkk(ee, k), mulkk(f, h))), mul(b, sub(mulkk(dd, k), mulkk(f, g)))),
                          mul(c, sub(mulkk(dd, h), mulkk(ee, g))))
                   << ";\n";
-                if (dfm && op == "inv") o << "        const " << W << " " << rd << " = ag::e64::recip(" << d << ");\n";
+                if (dfm && op == "inv") o << "        const " << W << " " << rd << " = " << NS << "recip(" << d << ");\n";
                 if (op == "det") {
                     e = {d};
                 } else {
@@ -866,12 +888,12 @@ struct Gen {
             const bool std01 = n.kids.size() > 1 && K(0).op == "lit" && K(0).lit == 0.0 && K(1).op == "lit" &&
                                K(1).lit == 1.0;
             auto u01 = [&](const char* salt, const std::string& cc) {
-                return dfm ? "ag::e64::draw01_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
+                return dfm ? NS + "draw01_df(" + key + " ^ " + salt + ", " + gid + ", " + cc + ")"
                            : "ag::draw01(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
             };
             const bool nrm_u = std01 && root_to_double && id == P.root && n.op == "normal";
             auto nrm = [&](const char* salt, const std::string& cc) {
-                return dfm ? std::string(nrm_u ? "ag::e64::normal_df<true>(" : "ag::e64::normal_df(") + key + " ^ " +
+                return dfm ? std::string(nrm_u ? NS + "normal_df<true>(" : NS + "normal_df(") + key + " ^ " +
                                  salt + ", " + gid + ", " + cc + ")"
                            : "ag::drawn(" + wp + ", " + key + " ^ " + salt + ", " + gid + ", " + cc + ")";
             };
@@ -890,7 +912,7 @@ struct Gen {
                     e.push_back(div(neg(call("log", {u01("AG_SALT_EXPONENTIAL", cc)}, id)), x0));
                 } else {   // DistributionLeaf.h:380-385
                     const std::string u = u01("AG_SALT_BERNOULLI", cc);
-                    e.push_back("(" + (dfm ? "ag::e64::lt(" + u + ", " + x0 + ")" : "(" + u + " < " + x0 + ")") + " ? " +
+                    e.push_back("(" + (dfm ? NS + "lt(" + u + ", " + x0 + ")" : "(" + u + " < " + x0 + ")") + " ? " +
                                 lit(1.0) + " : " + lit(0.0) + ")");
                 }
             }
@@ -973,11 +995,13 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     // Emulated FP64 (math 1, f64 plans) and the precision form (math 2, f32
     // and ff plans): the tree is generated in double-float (the fast path) and
     // once more on the native FP64 pipe (the per-lane fallback).
-    const bool emu = (low.math == 1 && P.dst_dtype == DType::F64) || (low.math == 2 && P.dst_dtype != DType::F64);
+    // FP64-grade triple-float (math 3, f64 plans) takes the same frame.
+    const bool tfx = low.math == 3 && P.dst_dtype == DType::F64;
+    const bool emu = (low.math == 1 && P.dst_dtype == DType::F64) || (low.math == 2 && P.dst_dtype != DType::F64) || tfx;
     const bool prec = emu && P.dst_dtype != DType::F64;   // float storage, float-float working values
     const bool dst_ff = P.dst_dtype == DType::FF;
     if (dst_ff && !prec) fail("ff destinations are written by the precision form (math = 2)");
-    Gen g(P, low, ctx, emu, emu ? "d" : "t");
+    Gen g(P, low, ctx, emu, emu ? "d" : "t", false, tfx);
     g.root_to_double = emu && P.dst_dtype == DType::F64;
     const std::vector<std::string> root = g.emit(P.root);
     Lowering nat = low;
@@ -993,6 +1017,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         o << "// generated by aether_gb300 from an aether-ir/1 plan\n";
         o << "#include \"ag_device.cuh\"\n";
         if (low.math >= 1) o << "#include \"ag_emu64.cuh\"\n";
+        if (tfx) o << "#include \"ag_tf64.cuh\"\n";
         if (low.math >= 1 && draws_normals(P)) o << "#include \"ag_emu64_bm.cuh\"\n";
         o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
     }
@@ -1074,14 +1099,14 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
     // is left out when the magnitude bounds of the root keep every value of a
     // lane that passed its other checks inside [2^-88, 2^126).
     const std::string FW = emu ? "double" : W;
-    const bool out_safe = emu && g.lo_of(P.root) >= -88 && g.hi_of(P.root) <= 125;
+    const bool out_safe = emu && g.lo_of(P.root) >= (tfx ? -80 : -88) && g.hi_of(P.root) <= 125;
     for (int c = 0; c < P.dst_comps; ++c) {
         if (prec) {
             o << "        ag::e64::df fv" << c << " = " << root[size_t(c)] << ";\n";
             if (!out_safe) o << "        ok_ = ok_ && ag::e64::out_ok(fv" << c << ");\n";
         } else if (emu) {
-            o << "        double fv" << c << " = ag::e64::to_double(" << root[size_t(c)] << ");\n";
-            if (!out_safe) o << "        ok_ = ok_ && ag::e64::out_ok(" << root[size_t(c)] << ");\n";
+            o << "        double fv" << c << " = " << g.NS << "to_double(" << root[size_t(c)] << ");\n";
+            if (!out_safe) o << "        ok_ = ok_ && " << g.NS << "out_ok(" << root[size_t(c)] << ");\n";
         } else {
             o << "        const " << W << " fv" << c << " = " << root[size_t(c)] << ";\n";
         }

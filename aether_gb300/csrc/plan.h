@@ -56,7 +56,8 @@ struct Lowering {
     int ipt = 1;              // lane groups per thread per chunk
     int vec = 0;              // samples per lane group (0 = 16 bytes of the widest storage type)
     bool contract = true;     // allow FMA contraction of arithmetic nodes
-    int math = 0;             // 0 = native FP64 pipe, 1 = emulated FP64 on FP32/INT pipes
+    int math = 0;             // 0 = native FP64 pipe, 1 = emulated FP64 on FP32/INT pipes (double-float),
+                              // 2 = precision form (f32/ff storage), 3 = FP64-grade triple-float
     int min_blocks = 0;       // __launch_bounds__ second argument (0 = none)
 };
 

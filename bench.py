@@ -50,15 +50,18 @@ def peaks():
 
 def profile_figures():
     """Per-kernel figures from the committed ncu summaries (profiles/ncu_traffic.txt):
-    {kind: {"kernel": name, "bytes_per_sample": B, "inst_per_sample": I}}. Each
-    line reads `<kind> <kernel name> <dram bytes/sample> <thread instructions/sample>`."""
+    {kernel name: {"kernel": name, "bytes_per_sample": B, "inst_per_sample": I}},
+    and under each kind the first line of that kind. Each line reads
+    `<kind> <kernel name> <dram bytes/sample> <thread instructions/sample>`."""
     path = os.path.join(REPO, "profiles", "ncu_traffic.txt")
     out = {}
     try:
         for line in open(path):
             f = line.split()
             if len(f) == 4 and not line.startswith("#"):
-                out[f[0]] = {"kernel": f[1], "bytes_per_sample": float(f[2]), "inst_per_sample": float(f[3])}
+                rec = {"kernel": f[1], "bytes_per_sample": float(f[2]), "inst_per_sample": float(f[3])}
+                out.setdefault(f[0], rec)
+                out[f[1]] = rec
     except OSError:
         pass
     return out
@@ -153,7 +156,18 @@ def cpu_leg(steps, warmup, nthreads=0, expr_samples=1 << 23, fill_samples=1 << 2
     return gbs, t, nt, sample, (ins, d_out, z_out)
 
 
-def check_against_oracle(arrs, d, z, ins, d_ref, z_ref, math):
+LOWERINGS = {0: "native FP64", 1: "emulated FP64 (double-float)", 3: "FP64-grade (triple-float)"}
+
+
+def fill_math(math):
+    """The fill's lowering for an expression lowering: the normals of the
+    double-float draw are within the reference's own normal tolerance (1e-12
+    abs+rel, random/detail/Backend.h:44-51), so the FP64-grade step draws them
+    that way; native FP64 keeps native draws."""
+    return 0 if math == 0 else 1
+
+
+def check_against_oracle(arrs, d, z, ins, d_ref, z_ref, math, math_z=None):
     """The GPU step's results on the CPU leg's sample against the oracle's
     (same seeded inputs): inputs bit for bit, the expression in units of
     2^-53 of its term scale, the normals in the reference's abs+rel form,
@@ -167,20 +181,20 @@ def check_against_oracle(arrs, d, z, ins, d_ref, z_ref, math):
     scale = np.maximum(np.abs(np.sqrt(a * a + b * b) * np.log1p(np.abs(c))), np.abs(1.0 / np.sqrt(1.0 + d0 * d0)))
     e_expr = acc.term_scale_error_2m53(got, d_ref[:, :n], scale)
     e_norm = acc.abs_rel_error_2m53(z.data[:, :nz].cpu().numpy(), z_ref[:, :nz])
-    out = {"lowering": ["native FP64", "emulated FP64"][math], "inputs_bit_exact": bool(same_inputs),
+    math_z = fill_math(math) if math_z is None else math_z
+    out = {"lowering": LOWERINGS[math], "fill_lowering": LOWERINGS[math_z], "inputs_bit_exact": bool(same_inputs),
            "expr_samples": int(n), "expr_max_err_2m53_of_terms": round(e_expr, 2),
            "normal_samples": int(nz), "normal_max_err_2m53_abs_rel": round(e_norm, 2), "reference_normal_tol": 1e-12}
-    if math == 0:
-        # native: ulp of the largest term, the unit the native bound is stated in
+    nb = acc.NATIVE_NORMAL_BOUND_2M53 if math_z == 0 else acc.EMU_NORMAL_BOUND_2M53
+    if math in (0, 3):
+        # native and FP64-grade: ulp of the largest term, the unit the native bound is stated in
         e_ulp = acc.term_scale_error_ulp(got, d_ref[:, :n], scale)
         out.update({"expr_max_err_ulp_of_terms": round(e_ulp, 2), "expr_bound_ulp_of_terms": acc.NATIVE_EXPR_ULPS,
-                    "normal_bound_2m53": acc.NATIVE_NORMAL_BOUND_2M53,
-                    "within_bounds": bool(same_inputs and e_ulp <= acc.NATIVE_EXPR_ULPS and
-                                          e_norm <= acc.NATIVE_NORMAL_BOUND_2M53)})
+                    "normal_bound_2m53": nb,
+                    "within_bounds": bool(same_inputs and e_ulp <= acc.NATIVE_EXPR_ULPS and e_norm <= nb)})
     else:
-        out.update({"expr_bound_2m53": acc.EMU_EXPR_BOUND_2M53, "normal_bound_2m53": acc.EMU_NORMAL_BOUND_2M53,
-                    "within_bounds": bool(same_inputs and e_expr <= acc.EMU_EXPR_BOUND_2M53 and
-                                          e_norm <= acc.EMU_NORMAL_BOUND_2M53)})
+        out.update({"expr_bound_2m53": acc.EMU_EXPR_BOUND_2M53, "normal_bound_2m53": nb,
+                    "within_bounds": bool(same_inputs and e_expr <= acc.EMU_EXPR_BOUND_2M53 and e_norm <= nb)})
     return out
 
 
@@ -563,7 +577,7 @@ def kernel_roofline(name, kernel, nbytes, ms, peak, twin_gbs, prof, samples, clo
          "frac": round(achieved / peak, 4)}
     if twin_gbs:
         e["l2_resident_gbs"] = round(twin_gbs, 1)
-    p = prof.get(name)
+    p = prof.get(kernel) or prof.get(name)
     e["bound"] = "hbm"
     if p and p["kernel"] == kernel:
         e["traffic"] = round(p["bytes_per_sample"] * samples)
@@ -581,12 +595,14 @@ def kernel_roofline(name, kernel, nbytes, ms, peak, twin_gbs, prof, samples, clo
     return e
 
 
-def native_fp64_step(ag, arrs, d, z, expr, g, steps, stream, ref):
-    """The same step lowered to native FP64 (math 0: CUDA's FP64 functions on
-    the FP64 pipe, the reference's own precision), timed like the headline
-    and checked against the oracle on the CPU leg's slice."""
-    k_expr = ag.prepare(d, expr, math=0, tune=True)
-    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=0, tune=True)
+def lowered_step(ag, arrs, d, z, expr, g, steps, stream, ref, math):
+    """The same step in another lowering, timed like the headline and checked
+    against the oracle on the CPU leg's slice: native FP64 (math 0, CUDA's FP64
+    functions on the FP64 pipe) or FP64-grade triple-float (math 3, within the
+    native bound of the oracle; its fill draws double-float normals, inside the
+    reference's normal tolerance)."""
+    k_expr = ag.prepare(d, expr, math=math, tune=True)
+    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=fill_math(math), tune=True)
     for _ in range(2):
         k_expr()
         k_fill()
@@ -594,14 +610,15 @@ def native_fp64_step(ag, arrs, d, z, expr, g, steps, stream, ref):
     te, tf = statistics.mean(te), statistics.mean(tf)
     peak, _ = peaks()
     n_steps = max(3, min(steps, 5))
-    out = {"ms_per_step": round(total / n_steps, 4),
+    out = {"lowering": LOWERINGS[math], "fill_lowering": LOWERINGS[fill_math(math)],
+           "ms_per_step": round(total / n_steps, 4),
            "value": round((BYTES_EXPR + BYTES_FILL) / (total / n_steps * 1e-3) / 1e9, 2),
            "expr": {"kernel": k_expr.plan.name, "ms": round(te, 4), "gbs": round(BYTES_EXPR / (te * 1e-3) / 1e9, 1),
                     "frac": round(BYTES_EXPR / (te * 1e-3) / 1e9 / peak, 4)},
            "fill": {"kernel": k_fill.plan.name, "ms": round(tf, 4), "gbs": round(BYTES_FILL / (tf * 1e-3) / 1e9, 1),
                     "frac": round(BYTES_FILL / (tf * 1e-3) / 1e9 / peak, 4)}}
     if ref is not None:
-        out["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref, math=0)
+        out["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref, math=math)
     return out
 
 
@@ -617,6 +634,7 @@ def run_ours(args):
     from aether_gb300 import shard
 
     math_mode = args.math
+    math_z = fill_math(math_mode)
     stream = torch.cuda.current_stream()
     g = ag.Generator(7)
     arrs = [ag.Array("f64", (3,), N_EXPR) for _ in range(4)]
@@ -627,7 +645,7 @@ def run_ours(args):
     a, b, c, d0 = (x.view() for x in arrs)
     expr = ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c)) + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0)
     k_expr = ag.prepare(d, expr, math=math_mode, tune=not args.no_tune)
-    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=math_mode, tune=not args.no_tune)
+    k_fill = ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), math=math_z, tune=not args.no_tune)
     torch.cuda.synchronize()
 
     def step():
@@ -686,7 +704,7 @@ def run_ours(args):
             e_r = ag.cwiseSqrt(a_ * a_ + b_ * b_) * ag.cwiseLog1p(ag.cwiseAbs(c_)) + \
                 ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0_ * d0_)
             ke = ag.prepare(bo, e_r, math=math_mode, tune=not args.no_tune) if bo.n else None
-            kf = ag.prepare(bz, g.substream(4).normal(1, 0.0, 1.0), sample_offset=r * pitch_f, math=math_mode,
+            kf = ag.prepare(bz, g.substream(4).normal(1, 0.0, 1.0), sample_offset=r * pitch_f, math=math_z,
                             tune=not args.no_tune) if bz.n else None
             chunks.append((r * pitch_e, bo.n, r * pitch_f, bz.n, ke, kf))
         cap = arrs[0].capacity
@@ -772,7 +790,7 @@ def run_ours(args):
     # compute ceiling is the issue ceiling alone
     n_tw_f = min(N_FILL, 1 << 23)
     twin_e = None
-    twin_f = l2_twin_gbs(ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), n=n_tw_f, math=math_mode,
+    twin_f = l2_twin_gbs(ag.prepare(z, g.substream(4).normal(1, 0.0, 1.0), n=n_tw_f, math=math_z,
                                     tune=not args.no_tune), n_tw_f, 8)
     kernels = {
         "expr": kernel_roofline("expr", k_expr.plan.name + "_v", BYTES_EXPR, te, peak, twin_e, prof, N_EXPR,
@@ -797,17 +815,19 @@ def run_ours(args):
         gbs, t, nt, sample, ref = cpu_leg(1, 1)
         cpu = {"value": round(gbs, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample}
         # the oracle doubles as the checker of this run's GPU results
-        cpu["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref, math=math_mode)
+        cpu["gpu_vs_oracle"] = check_against_oracle(arrs, d, z, *ref, math=math_mode, math_z=math_z)
     secondary = None
     if not args.no_secondary:
         # the other configurations, measured after the timed region
         secondary = {}
         wanted = set(args.secondary.split(",")) if args.secondary else None
-        if math_mode != 0 and (wanted is None or "native_fp64_step" in wanted):
+        for name, m in (("native_fp64_step", 0), ("fp64_grade_step", 3)):
+            if math_mode == m or (wanted is not None and name not in wanted):
+                continue
             try:
-                secondary["native_fp64_step"] = native_fp64_step(ag, arrs, d, z, expr, g, args.steps, stream, ref)
+                secondary[name] = lowered_step(ag, arrs, d, z, expr, g, args.steps, stream, ref, m)
             except Exception as ex:   # reported, never hidden
-                secondary["native_fp64_step"] = {"error": str(ex).splitlines()[0][:300] if str(ex) else repr(ex)}
+                secondary[name] = {"error": str(ex).splitlines()[0][:300] if str(ex) else repr(ex)}
         for name, fn in (("config1_plain", secondary_config1), ("config3_precision_form", secondary_config3),
                          ("config4_batch", secondary_config4), ("config5_serving", secondary_config5)):
             if wanted is not None and name not in wanted:
@@ -821,7 +841,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 seed 7, generated on device)",
         "config": {"workload": WORKLOAD, "samples_expr": N_EXPR, "samples_fill": N_FILL,
-                   "l2": "inputs larger than L2 (no flush)", "math": ["native FP64", "emulated FP64"][math_mode],
+                   "l2": "inputs larger than L2 (no flush)", "math": LOWERINGS[math_mode], "fill_math": LOWERINGS[math_z],
                    "lowering_expr": {"block": k_expr.plan.info().block, "ipt": k_expr.plan.info().ipt,
                                      "vec": k_expr.plan.info().vec, "registers": k_expr.plan.info().registers},
                    "lowering_fill": {"block": k_fill.plan.info().block, "ipt": k_fill.plan.info().ipt,
@@ -842,14 +862,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--math", type=int, default=1, help="0 native FP64, 1 emulated FP64")
+    ap.add_argument("--math", type=int, default=1, choices=[0, 1, 3],
+                    help="lowering of the expression: 0 native FP64, 1 emulated FP64 (double-float), "
+                         "3 FP64-grade (triple-float); the fill follows (native for 0, double-float otherwise)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default lowering instead of the autotuned one")
     ap.add_argument("--no-secondary", action="store_true", help="skip configs 1, 3, 4 and 5 after the timed region")
     ap.add_argument("--e2e-chunks", type=int, default=4, help="sample blocks of the pipelined end-to-end step")
     ap.add_argument("--secondary", default="", help="comma-separated subset of the secondary measurements "
-                                                     "(native_fp64_step, config1_plain, config3_precision_form, "
+                                                     "(native_fp64_step, fp64_grade_step, config1_plain, "
+                                                     "config3_precision_form, "
                                                      "config4_batch, config5_serving); default all")
     ap.add_argument("--expr-log2", type=int, default=26, help="log2 samples of the expression kernel")
     ap.add_argument("--fill-log2", type=int, default=28, help="log2 doubles of the normal fill")

@@ -120,7 +120,9 @@ typedef struct AetherLowering {
     int contract;     /* 1: FMA contraction allowed, 0: every add/mul rounds (-fmad=false), -1: default (1) */
     int math;         /* 0: FP64 on the FP64 pipe; 1: FP64 emulated on the FP32/INT pipes (double-float);
                          2: the precision form -- f32 or float-float storage evaluated in double-float
-                         arithmetic, exact products of f32 operands, FP64 only in the final stage of sums */
+                         arithmetic, exact products of f32 operands, FP64 only in the final stage of sums;
+                         3: FP64-grade on the FP32/INT pipes (triple-float, f64 plans): doubles split exactly
+                         into three floats, results within an ulp or so of the native pipe's */
     int min_blocks;   /* __launch_bounds__ min blocks per SM */
 } AetherLowering;
 

@@ -87,10 +87,11 @@ def _corpus():
 
 
 @pytest.mark.parametrize("case", list(_corpus()), ids=lambda c: c[0])
-@pytest.mark.parametrize("contract, math", [(0, 0), (1, 0), (0, 1), (0, 2)])
+@pytest.mark.parametrize("contract, math", [(0, 0), (1, 0), (0, 1), (0, 2), (0, 3)])
 def test_corpus_lowers_and_compiles_for_sm103a(case, contract, math):
-    # math 1 (double-float for f64 plans) and 2 (float-float for f32/ff
-    # plans) lower the same corpus through the emulated generator
+    # math 1 (double-float for f64 plans), 2 (float-float for f32/ff plans)
+    # and 3 (triple-float for f64 plans) lower the same corpus through the
+    # emulated generator
     name, dt, shape, op, e = case
     ir = plan_text(dt, shape, op, e, IrContext())
     src = _abi.generate(ir, _abi.lowering(contract=contract, math=math))

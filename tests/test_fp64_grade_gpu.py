@@ -1,0 +1,177 @@
+"""GPU parity of the FP64-grade lowering (math = 3, ag_tf64.cuh): f64 plans
+evaluated in triple-float arithmetic on the FP32/INT pipes.
+
+Bounds (aether_gb300.accuracy): against exact arithmetic (long double, at
+least 64 significant bits) FP64_GRADE_EXACT_ULPS ulps of the term scale;
+against the oracle and the reference's own outputs (double arithmetic, a few
+ulps from exact themselves) the native bound NATIVE_EXPR_ULPS. Samples outside
+the triple-float range take the native FP64 kernel bit for bit; Philox fills
+are bit-exact (uniforms exactly representable, normals from the native draw).
+"""
+
+import numpy as np
+import pytest
+
+from conftest import assert_ulp
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+
+
+import aether_gb300 as ag
+from aether_gb300.accuracy import FP64_GRADE_EXACT_ULPS, NATIVE_EXPR_ULPS
+
+
+def dev_array(host):
+    host = np.asarray(host)
+    if host.ndim == 1:
+        host = host[None, :]
+    arr = ag.Array("f64", (host.shape[0],), host.shape[1])
+    arr.upload(host)
+    return arr
+
+
+def _cfg2a(a, b, c, d0):
+    return ag.cwiseSqrt(a * a + b * b) * ag.cwiseLog1p(ag.cwiseAbs(c)) + ag.cwiseRsqrt(ag.constant(1.0, (3,)) + d0 * d0)
+
+
+def _cfg1(a, b, c):
+    return a + b * c + ag.cwiseSin(a) * ag.cwiseExp((c * c) * (-1.0))
+
+
+def _cfg2a_exact(A, B, C, D0):
+    L = [np.asarray(x, dtype=np.longdouble) for x in (A, B, C, D0)]
+    a, b, c, d0 = L
+    t1 = np.sqrt(a * a + b * b) * np.log1p(np.abs(c))
+    t2 = 1 / np.sqrt(1 + d0 * d0)
+    return t1 + t2, np.maximum(np.abs(t1), np.abs(t2))
+
+
+def _ulps_of_scale(got, exact, scale):
+    sp = np.spacing(np.asarray(scale, dtype=np.float64))
+    return float(np.max(np.abs(np.asarray(got, dtype=np.longdouble) - exact) / sp.astype(np.longdouble)))
+
+
+def test_config2a_against_reference_and_exact(ref_cases):
+    z = ref_cases
+    cols = [z[k] for k in ("cfg2a_a", "cfg2a_b", "cfg2a_c", "cfg2a_d0")]
+    ins = [dev_array(x) for x in cols]
+    d = ag.Array("f64", (3,), 1000)
+    ag.assign(d, _cfg2a(*(x.view() for x in ins)), math=3)
+    exact, scale = _cfg2a_exact(*cols)
+    assert_ulp(d.host(), z["cfg2a_d"], NATIVE_EXPR_ULPS, scale.astype(np.float64), "config 2a FP64-grade vs reference")
+    assert _ulps_of_scale(d.host(), exact, scale) <= FP64_GRADE_EXACT_ULPS
+
+
+def test_config2a_full_size_subsample(oracle):
+    n = 1 << 24
+    arrs = [ag.Array("f64", (3,), n) for _ in range(4)]
+    for k, arr in enumerate(arrs):
+        ag.assign(arr, ag.Generator(7).substream(k).uniform(3, -4.0, 4.0), math=3)
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, _cfg2a(*(x.view() for x in arrs)), math=3)
+    idx = torch.randint(0, n, (1 << 15,), generator=torch.Generator().manual_seed(3)).cuda()
+    sub = [np.ascontiguousarray(x.data[:, idx].cpu().numpy()) for x in arrs]
+    got = d.data[:, idx].cpu().numpy()
+    exact, scale = _cfg2a_exact(*sub)
+    assert_ulp(got, oracle.cfg2a(*sub), NATIVE_EXPR_ULPS, scale.astype(np.float64), "config 2a FP64-grade, 2^24")
+    assert _ulps_of_scale(got, exact, scale) <= FP64_GRADE_EXACT_ULPS
+
+
+def test_config1_against_reference(ref_cases):
+    z = ref_cases
+    a, b, c = (dev_array(z[k]) for k in ("cfg1_a", "cfg1_b", "cfg1_c"))
+    d = ag.Array("f64", (3,), 1000)
+    ag.assign(d, _cfg1(a.view(), b.view(), c.view()), math=3)
+    A, B, C = z["cfg1_a"], z["cfg1_b"], z["cfg1_c"]
+    scale = np.maximum.reduce([np.abs(A), np.abs(B * C), np.abs(np.sin(A) * np.exp(-C * C))])
+    assert_ulp(d.host(), z["cfg1_d"], NATIVE_EXPR_ULPS, scale, "config 1 FP64-grade vs reference")
+
+
+@pytest.mark.parametrize("name", ["cross", "qrot", "inv_guard", "div_mix", "log_mix"])
+def test_nodes_against_native(name):
+    """Geometry, guarded inverse and quotients: within the native bound of the
+    native lowering on the same inputs (well-conditioned samples)."""
+    n = 8192
+    g = ag.Generator(19)
+    a, b = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
+    q, m = ag.Array("f64", (4,), n), ag.Array("f64", (3, 3), n)
+    ag.assign(a, g.substream(0).uniform(3, -2.0, 2.0))
+    ag.assign(b, g.substream(1).uniform(3, 0.5, 3.0))
+    ag.assign(q, g.substream(2).uniform(4, -1.0, 1.0))
+    ag.assign(m, g.substream(3).uniform(9, -1.0, 1.0).reshape((3, 3)))
+    A, B, Q, M = a.view(), b.view(), q.view(), m.view()
+    e, shape = {
+        "cross": (A.cross(B), (3,)),
+        "qrot": (Q.quatRotate(A), (3,)),
+        "inv_guard": (ag.select(ag.cwiseAbs(M.det()) > 1e-300, M.inverse(), ag.constant(0.0, (3, 3))), (3, 3)),
+        "div_mix": (ag.cwiseDiv(A, B) + A * (1.0 / 3.0), (3,)),
+        "log_mix": (ag.cwiseLog(B) - ag.cwiseSqrt(B) * ag.cwiseRsqrt(B + A * A), (3,)),
+    }[name]
+    d3, d0 = ag.Array("f64", shape, n), ag.Array("f64", shape, n)
+    ag.assign(d3, e, math=3)
+    ag.assign(d0, e, math=0, contract=0)
+    got, nat = d3.host(), d0.host()
+    if name == "inv_guard":
+        H = m.host()
+        keep = np.abs(np.linalg.det(H.T.reshape(n, 3, 3))) > 1e-2
+        scale = np.abs(nat[:, keep]).max(axis=0)
+        assert np.all(np.abs(got[:, keep] - nat[:, keep]) <= 16 * np.spacing(scale))
+    else:
+        assert_ulp(got, nat, NATIVE_EXPR_ULPS, None, name)
+
+
+def test_fallback_reproduces_native_on_special_inputs():
+    """Zeros, denormals, huge values, infinities and NaNs leave the
+    triple-float range: those samples are the native kernel's bit for bit."""
+    special = np.array([0.0, -0.0, 1e-310, -1e-200, 1e-30, 1e30, 1e200, np.inf, -np.inf, np.nan, 3.0, -2.5,
+                        2.0 ** -41, 2.0 ** 61, 1e-11, 7.0], dtype=np.float64)
+    n = special.size
+    rng = np.random.default_rng(5)
+    cols = [np.stack([rng.permutation(special) for _ in range(3)]) for _ in range(4)]
+    ins = [dev_array(c) for c in cols]
+    e = _cfg2a(*(x.view() for x in ins))
+    d_nat, d_tf = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
+    ag.assign(d_nat, e, math=0, contract=1)
+    ag.assign(d_tf, e, math=3)
+    got, nat = d_tf.host(), d_nat.host()
+    inrange = np.all([(np.abs(x) >= 2.0 ** -40) & (np.abs(x) <= 2.0 ** 60) for x in cols], axis=0)
+    assert np.array_equal(got[~inrange], nat[~inrange], equal_nan=True)
+    with np.errstate(all="ignore"):
+        exact, scale = _cfg2a_exact(*cols)
+    assert _ulps_of_scale(got[inrange], exact[inrange], scale[inrange]) <= FP64_GRADE_EXACT_ULPS
+
+
+def test_fills_are_exact(oracle):
+    n = 100003
+    a = ag.Array("f64", (3,), n)
+    ag.assign(a, ag.Generator(7).substream(0).uniform(3, -4.0, 4.0), math=3)
+    key = oracle.substream_key(oracle.generator_key(7), 0)
+    assert np.array_equal(a.host(), oracle.fill_uniform_f64(key, -4.0, 4.0, 3, n))
+    y3, y0 = ag.Array("f64", (1,), n), ag.Array("f64", (1,), n)
+    ag.assign(y3, ag.Generator(7).substream(4).normal(1, 0.0, 1.0), math=3)
+    ag.assign(y0, ag.Generator(7).substream(4).normal(1, 0.0, 1.0), math=0)
+    assert np.array_equal(y3.host(), y0.host())
+
+
+def test_scalars_and_literals_keep_their_bits():
+    """A runtime scalar and a literal that need all 53 bits (1/3, pi) enter
+    exactly: a * s - a * s is zero and (a + s) - s returns a."""
+    n = 4096
+    a = ag.Array("f64", (1,), n)
+    ag.assign(a, ag.Generator(3).uniform(1, 1.0, 2.0))
+    s = 1.0 / 3.0
+    d = ag.Array("f64", (1,), n)
+    ag.assign(d, (a.view() + s) - s, math=3)
+    assert_ulp(d.host(), a.host(), 1, None, "(a + 1/3) - 1/3")
+    ag.assign(d, a.view() * ag.literal(np.pi), math=3)
+    ref = (a.host().astype(np.longdouble) * np.longdouble(np.pi))
+    assert np.max(np.abs(d.host() - ref) / np.spacing(np.abs(d.host()))) <= 0.5 + 1e-6
