@@ -41,17 +41,23 @@ def _device_name():
     return torch.cuda.get_device_name(torch.cuda.current_device())
 
 
-def _code_digest():
-    """Digest of the device runtime every generated kernel includes (the
-    payload headers under their bare names; the consumer headers under
-    aether/ never reach a generated kernel): a tuning result stays valid only
-    for the code it was measured on."""
+# Device headers only FP64-grade (math 3) kernels include.
+_TF_HEADERS = ("ag_tf64.cuh", "ag_tf64_tables.cuh")
+
+
+def _code_digest(math=0):
+    """Digest of the device runtime a generated kernel of this lowering can
+    include (the payload headers under their bare names; the consumer headers
+    under aether/ never reach a generated kernel, and the triple-float headers
+    only reach math-3 kernels): a tuning result stays valid only for the code
+    it was measured on."""
     from . import rtc
     h = hashlib.sha1()
     for name, src in sorted(rtc.payload().headers.items()):
-        if not name.startswith("aether/"):
-            h.update(name.encode())
-            h.update(src)
+        if name.startswith("aether/") or (name in _TF_HEADERS and math != 3):
+            continue
+        h.update(name.encode())
+        h.update(src)
     return h.hexdigest()[:16]
 
 
@@ -72,7 +78,7 @@ def _key(ir, math, contract, regime=""):
     measured at: "" for whole-array launches (the benchmarks' 2^26..2^28
     samples), "serve" for served requests (2^21 samples), whose winners differ
     (tail effects favour smaller blocks)."""
-    h = hashlib.sha1(("%s|%d|%d|%s|%s|%s" % (ir, math, contract, _device_name(), _code_digest(),
+    h = hashlib.sha1(("%s|%d|%d|%s|%s|%s" % (ir, math, contract, _device_name(), _code_digest(math),
                                              _generated_digest(ir, math, contract))).encode()).hexdigest()
     return regime_key(h, regime)
 

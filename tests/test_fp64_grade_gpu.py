@@ -96,37 +96,68 @@ def test_config1_against_reference(ref_cases):
     assert_ulp(d.host(), z["cfg1_d"], NATIVE_EXPR_ULPS, scale, "config 1 FP64-grade vs reference")
 
 
-@pytest.mark.parametrize("name", ["cross", "qrot", "inv_guard", "div_mix", "log_mix"])
-def test_nodes_against_native(name):
-    """Geometry, guarded inverse and quotients: within the native bound of the
-    native lowering on the same inputs (well-conditioned samples)."""
+def _q(x):
+    return np.asarray(x, dtype=np.longdouble)
+
+
+@pytest.mark.parametrize("name", ["cross", "qrot", "div_mix", "log_mix"])
+def test_nodes_against_exact(name):
+    """Geometry, quotients and logarithms against long-double evaluation of
+    the same formula, in ulps of each sample's term scale (the largest
+    magnitude among the terms its sums combine)."""
     n = 8192
     g = ag.Generator(19)
-    a, b = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
-    q, m = ag.Array("f64", (4,), n), ag.Array("f64", (3, 3), n)
+    a, b, q = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n), ag.Array("f64", (4,), n)
     ag.assign(a, g.substream(0).uniform(3, -2.0, 2.0))
     ag.assign(b, g.substream(1).uniform(3, 0.5, 3.0))
     ag.assign(q, g.substream(2).uniform(4, -1.0, 1.0))
-    ag.assign(m, g.substream(3).uniform(9, -1.0, 1.0).reshape((3, 3)))
-    A, B, Q, M = a.view(), b.view(), q.view(), m.view()
-    e, shape = {
-        "cross": (A.cross(B), (3,)),
-        "qrot": (Q.quatRotate(A), (3,)),
-        "inv_guard": (ag.select(ag.cwiseAbs(M.det()) > 1e-300, M.inverse(), ag.constant(0.0, (3, 3))), (3, 3)),
-        "div_mix": (ag.cwiseDiv(A, B) + A * (1.0 / 3.0), (3,)),
-        "log_mix": (ag.cwiseLog(B) - ag.cwiseSqrt(B) * ag.cwiseRsqrt(B + A * A), (3,)),
-    }[name]
-    d3, d0 = ag.Array("f64", shape, n), ag.Array("f64", shape, n)
-    ag.assign(d3, e, math=3)
-    ag.assign(d0, e, math=0, contract=0)
-    got, nat = d3.host(), d0.host()
-    if name == "inv_guard":
-        H = m.host()
-        keep = np.abs(np.linalg.det(H.T.reshape(n, 3, 3))) > 1e-2
-        scale = np.abs(nat[:, keep]).max(axis=0)
-        assert np.all(np.abs(got[:, keep] - nat[:, keep]) <= 16 * np.spacing(scale))
+    A, B, Q = a.view(), b.view(), q.view()
+    HA, HB, HQ = _q(a.host()), _q(b.host()), _q(q.host())
+    if name == "cross":
+        e = A.cross(B)
+        terms = [HA[1] * HB[2], HA[2] * HB[1], HA[2] * HB[0], HA[0] * HB[2], HA[0] * HB[1], HA[1] * HB[0]]
+        exact = np.stack([terms[0] - terms[1], terms[2] - terms[3], terms[4] - terms[5]])
+        scale = np.stack([np.maximum(abs(terms[0]), abs(terms[1])), np.maximum(abs(terms[2]), abs(terms[3])),
+                          np.maximum(abs(terms[4]), abs(terms[5]))])
+    elif name == "qrot":
+        e = Q.quatRotate(A)
+        w, x, y, z = HQ
+        # v' = v + 2 w (u x v) + 2 u x (u x v), u = (x, y, z)
+        u = np.stack([x, y, z])
+        uv = np.stack([u[1] * HA[2] - u[2] * HA[1], u[2] * HA[0] - u[0] * HA[2], u[0] * HA[1] - u[1] * HA[0]])
+        uuv = np.stack([u[1] * uv[2] - u[2] * uv[1], u[2] * uv[0] - u[0] * uv[2], u[0] * uv[1] - u[1] * uv[0]])
+        exact = HA + 2 * w * uv + 2 * uuv
+        # every term is at most |v| (1 + 4 |q|^2) in magnitude
+        scale = np.broadcast_to(np.sqrt((HA * HA).sum(axis=0)) * (1 + 4 * (w * w + x * x + y * y + z * z)), exact.shape)
+    elif name == "div_mix":
+        e = ag.cwiseDiv(A, B) + A * (1.0 / 3.0)
+        exact = HA / HB + HA * _q(1.0 / 3.0)
+        scale = np.maximum(abs(HA / HB), abs(HA) / 3)
     else:
-        assert_ulp(got, nat, NATIVE_EXPR_ULPS, None, name)
+        e = ag.cwiseLog(B) - ag.cwiseSqrt(B) * ag.cwiseRsqrt(B + A * A)
+        t2 = np.sqrt(HB) / np.sqrt(HB + HA * HA)
+        exact = np.log(HB) - t2
+        scale = np.maximum(abs(np.log(HB)), abs(t2))
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, e, math=3)
+    err = _ulps_of_scale(d.host(), exact, np.asarray(scale, dtype=np.float64))
+    assert err <= FP64_GRADE_EXACT_ULPS, (name, err)
+
+
+def test_guarded_inverse_against_native():
+    n = 8192
+    m = ag.Array("f64", (3, 3), n)
+    ag.assign(m, ag.Generator(8).uniform(9, -1.0, 1.0).reshape((3, 3)))
+    M = m.view()
+    e = ag.select(ag.cwiseAbs(M.det()) > 1e-300, M.inverse(), ag.constant(0.0, (3, 3)))
+    d3, d0 = ag.Array("f64", (3, 3), n), ag.Array("f64", (3, 3), n)
+    ag.assign(d3, e, math=3)
+    ag.assign(d0, e, math=0)
+    got, nat = d3.host(), d0.host()
+    H = m.host()
+    keep = np.abs(np.linalg.det(H.T.reshape(n, 3, 3))) > 1e-2   # well-conditioned matrices
+    scale = np.abs(nat[:, keep]).max(axis=0)
+    assert np.all(np.abs(got[:, keep] - nat[:, keep]) <= 2.0 ** -40 * scale)
 
 
 def test_fallback_reproduces_native_on_special_inputs():
