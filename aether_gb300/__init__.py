@@ -236,7 +236,7 @@ class Plan:
     def name(self):
         """The kernel's base name (its vectorised and scalar kernels add _v / _s)."""
         import re
-        m = re.search(r"\b(ag_(?:expr|fill|sum)_[0-9a-f]{8})_v\b", self.source())
+        m = re.search(r"\b(ag_(?:expr|fill|sum)_[0-9a-f]{8}(?:_tf)?)_v\b", self.source())
         return m.group(1) if m else None
 
     def workspace_size(self, n):

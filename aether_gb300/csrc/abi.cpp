@@ -29,6 +29,13 @@
 
 namespace {
 
+// Kernels of the FP64-grade lowering carry a _tf tag, so profiles and launch
+// lists tell them from the double-float kernels of the same expression.
+std::string lowering_tag(const ag::Plan& plan, const ag::Lowering& low) {
+    return low.math == 3 && plan.dst_dtype == ag::DType::F64 ? "_tf" : "";
+}
+
+
 thread_local std::string g_error;
 
 int fail(const std::string& m) {
@@ -334,7 +341,7 @@ AG_EXPORT int aether_plan_create(const char* ir, const AetherLowering* lowering,
         if (P->low.math == 3 && P->plan.dst_dtype != ag::DType::F64)
             throw std::runtime_error("plan_create: FP64-grade triple-float (math = 3) applies to f64 plans");
         if (P->low.math < 0 || P->low.math > 3) throw std::runtime_error("plan_create: math must be 0, 1, 2 or 3");
-        P->name = ag::kernel_base(P->plan, ir);
+        P->name = ag::kernel_base(P->plan, ir) + lowering_tag(P->plan, P->low);
         P->source = ag::generate_source(P->plan, P->low, P->name);
         ck(cudaFree(nullptr), "CUDA context");   // make the primary context current
         cudaGetDevice(&P->dev);
@@ -750,7 +757,7 @@ AG_EXPORT int aether_plan_generate(const char* ir, const AetherLowering* lowerin
             if (lowering->math >= 0) low.math = lowering->math;
             if (lowering->min_blocks > 0) low.min_blocks = lowering->min_blocks;
         }
-        const std::string src = ag::generate_source(plan, low, ag::kernel_base(plan, ir));
+        const std::string src = ag::generate_source(plan, low, ag::kernel_base(plan, ir) + lowering_tag(plan, low));
         if (len) *len = src.size();
         if (buf && cap) {
             const size_t n = std::min(cap - 1, src.size());

@@ -95,7 +95,9 @@ def test_corpus_lowers_and_compiles_for_sm103a(case, contract, math):
     name, dt, shape, op, e = case
     ir = plan_text(dt, shape, op, e, IrContext())
     src = _abi.generate(ir, _abi.lowering(contract=contract, math=math))
-    assert re.search(r"ag_(expr|fill|sum)_[0-9a-f]{8}_v\(", src) and re.search(r"ag_(expr|fill|sum)_[0-9a-f]{8}_s\(", src)
+    assert re.search(r"ag_(expr|fill|sum)_[0-9a-f]{8}(_tf)?_v\(", src) and re.search(r"ag_(expr|fill|sum)_[0-9a-f]{8}(_tf)?_s\(", src)
+    if math == 3 and dt == "f64":
+        assert "_tf_v(" in src
     _abi.nvrtc_check(src, "sm_103a")
 
 
