@@ -595,7 +595,7 @@ def kernel_roofline(name, kernel, nbytes, ms, peak, twin_gbs, prof, samples, clo
     return e
 
 
-def lowered_step(ag, arrs, d, z, expr, g, steps, stream, ref, math):
+def lowered_step(ag, arrs, d, z, expr, g, steps, stream, ref, math, clock_mhz=None, sms=152):
     """The same step in another lowering, timed like the headline and checked
     against the oracle on the CPU leg's slice: native FP64 (math 0, CUDA's FP64
     functions on the FP64 pipe) or FP64-grade triple-float (math 3, within the
@@ -614,7 +614,9 @@ def lowered_step(ag, arrs, d, z, expr, g, steps, stream, ref, math):
            "ms_per_step": round(total / n_steps, 4),
            "value": round((BYTES_EXPR + BYTES_FILL) / (total / n_steps * 1e-3) / 1e9, 2),
            "expr": {"kernel": k_expr.plan.name, "ms": round(te, 4), "gbs": round(BYTES_EXPR / (te * 1e-3) / 1e9, 1),
-                    "frac": round(BYTES_EXPR / (te * 1e-3) / 1e9 / peak, 4)},
+                    "frac": round(BYTES_EXPR / (te * 1e-3) / 1e9 / peak, 4),
+                    "roofline": kernel_roofline("expr", k_expr.plan.name + "_v", BYTES_EXPR, te, peak, None,
+                                                profile_figures(), N_EXPR, clock_mhz, sms)},
            "fill": {"kernel": k_fill.plan.name, "ms": round(tf, 4), "gbs": round(BYTES_FILL / (tf * 1e-3) / 1e9, 1),
                     "frac": round(BYTES_FILL / (tf * 1e-3) / 1e9 / peak, 4)}}
     if ref is not None:
@@ -825,7 +827,8 @@ def run_ours(args):
             if math_mode == m or (wanted is not None and name not in wanted):
                 continue
             try:
-                secondary[name] = lowered_step(ag, arrs, d, z, expr, g, args.steps, stream, ref, m)
+                secondary[name] = lowered_step(ag, arrs, d, z, expr, g, args.steps, stream, ref, m,
+                                               clocks.get("sm_mhz"), props.multi_processor_count)
             except Exception as ex:   # reported, never hidden
                 secondary[name] = {"error": str(ex).splitlines()[0][:300] if str(ex) else repr(ex)}
         for name, fn in (("config1_plain", secondary_config1), ("config3_precision_form", secondary_config3),

@@ -24,8 +24,9 @@ namespace aether {
 namespace gb300 {
 
 /** Lowering of the kernels this front end compiles. math: 0 FP64 on the FP64
- *  pipe, 1 FP64 emulated on the FP32/INT pipes (double plans), 2 FP32 storage
- *  with float-float arithmetic (float plans), -1 the default for the
+ *  pipe, 1 FP64 emulated on the FP32/INT pipes (double-float, double plans),
+ *  2 FP32 storage with float-float arithmetic (float plans), 3 FP64-grade
+ *  triple-float on the FP32/INT pipes (double plans), -1 the default for the
  *  destination type (0 for double, 2 for float). contract: 1 FMA contraction,
  *  0 every add and mul rounds, -1 default. Other fields <= 0: tuned default. */
 struct Lowering {

@@ -165,9 +165,12 @@ def test_fallback_reproduces_native_on_special_inputs():
     triple-float range: those samples are the native kernel's bit for bit."""
     special = np.array([0.0, -0.0, 1e-310, -1e-200, 1e-30, 1e30, 1e200, np.inf, -np.inf, np.nan, 3.0, -2.5,
                         2.0 ** -41, 2.0 ** 61, 1e-11, 7.0], dtype=np.float64)
-    n = special.size
     rng = np.random.default_rng(5)
-    cols = [np.stack([rng.permutation(special) for _ in range(3)]) for _ in range(4)]
+    # the specials mixed across the four operands, then samples with every
+    # operand in range, so both sides of the range test occur
+    cols = [np.concatenate([np.stack([rng.permutation(special) for _ in range(3)]),
+                            rng.uniform(-4.0, 4.0, size=(3, 64))], axis=1) for _ in range(4)]
+    n = cols[0].shape[1]
     ins = [dev_array(c) for c in cols]
     e = _cfg2a(*(x.view() for x in ins))
     d_nat, d_tf = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
@@ -175,6 +178,7 @@ def test_fallback_reproduces_native_on_special_inputs():
     ag.assign(d_tf, e, math=3)
     got, nat = d_tf.host(), d_nat.host()
     inrange = np.all([(np.abs(x) >= 2.0 ** -40) & (np.abs(x) <= 2.0 ** 60) for x in cols], axis=0)
+    assert (~inrange).any() and inrange.any()
     assert np.array_equal(got[~inrange], nat[~inrange], equal_nan=True)
     with np.errstate(all="ignore"):
         exact, scale = _cfg2a_exact(*cols)
