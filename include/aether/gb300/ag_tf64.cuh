@@ -88,6 +88,16 @@ __device__ __forceinline__ tf add_fast(tf a, tf b) {
     const df w = fast_two_sum(s.hi, u.hi);
     return mk3(w.hi, w.lo, z);
 }
+// a + b where a leads: |a.x| >= |b.x| (or a.x = 0) and |a + b| >= |a| / 2, so
+// the leading floats join by Fast2Sum and the result cannot cancel.
+__device__ __forceinline__ tf add_lead(tf a, tf b) {
+    const df s = fast_two_sum(a.x, b.x);
+    const df t = two_sum(a.y, b.y);
+    const df u = two_sum(s.lo, t.hi);
+    const float z = __fadd_rn(__fadd_rn(t.lo, u.lo), __fadd_rn(a.z, b.z));
+    const df w = fast_two_sum(s.hi, u.hi);
+    return mk3(w.hi, w.lo, z);
+}
 // The reassembly into a double rounds x + y + z once whatever their overlap,
 // so the root of a plan has no cheaper form here.
 __device__ __forceinline__ tf add_fast_u(tf a, tf b) { return add_fast(a, b); }
@@ -121,6 +131,15 @@ __device__ __forceinline__ tf sqr(tf a) {
     const float r = __fmaf_rn(a.y, a.y, __fmul_rn(x2, a.z));
     const df u = two_sum(p.lo, q.hi);
     const float z = __fadd_rn(__fadd_rn(q.lo, u.lo), r);
+    const df w = fast_two_sum(p.hi, u.hi);
+    return mk3(w.hi, w.lo, z);
+}
+// The square of a double-float as a triple-float (no third input float).
+__device__ __forceinline__ tf sqr_df(df a) {
+    const df p = two_prod(a.hi, a.hi);
+    const df q = two_prod(__fmul_rn(2.0f, a.hi), a.lo);
+    const df u = two_sum(p.lo, q.hi);
+    const float z = __fmaf_rn(a.lo, a.lo, __fadd_rn(q.lo, u.lo));
     const df w = fast_two_sum(p.hi, u.hi);
     return mk3(w.hi, w.lo, z);
 }
@@ -247,7 +266,7 @@ __device__ __forceinline__ tf sqrt_nn_(tf a) { return sqrt_(a); }
 // e = 1 - a y^2 formed like the reciprocal's residual.
 __device__ __forceinline__ tf rsqrt_(tf a) {
     const df y = e64::rsqrt_(mk(a.x, a.y));
-    const tf m = mul(a, sqr(from_df(y)));
+    const tf m = mul(a, sqr_df(y));
     const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, m.x), m.y), m.z);
     return mk3(y.hi, y.lo, __fmul_rn(__fmul_rn(y.hi, e), 0.5f));
 }
@@ -300,9 +319,11 @@ __device__ __forceinline__ tf log_s(float s, tf a) {
     const df h = fast_two_sum(t.x, P.hi);
     const df k = two_sum(h.lo, t.y);
     const tf T = mk3(h.hi, k.hi, __fadd_rn(__fadd_rn(k.lo, t.z), P.lo));
-    // e ln2 - log c_i, each from its table as three floats
+    // e ln2 - log c_i, each from its table as three floats. |e ln2| >= ln2 >
+    // 0.29 >= |log c_i| unless e = 0, and |-log c_i| >= 2^-10 >= 2 |T| unless
+    // i = 0 (then the leading term is 0): both sums are led by their first term.
     const e64::f4 ep = e64::ld4(kLn2Mul3, e + AG_TF_LN2_TAB_OFF);
-    const tf res = add(add(mk3(ep.x, ep.y, ep.z), mk3(cl.y, cl.z, cl.w)), T);
+    const tf res = add_lead(add_lead(mk3(ep.x, ep.y, ep.z), mk3(cl.y, cl.z, cl.w)), T);
     if (!checked) return res;
     const bool valid = yh > 0.0f && e > -120 && e < 120;
     return valid ? res : mk3(__int_as_float(0x7fc00000), 0.0f, 0.0f);
