@@ -1247,6 +1247,9 @@ std::string generate_batch_source(const std::vector<const Plan*>& plans, const s
     bool bm = false;
     for (size_t p = 0; p < plans.size(); ++p) bm = bm || (lows[p].math >= 1 && draws_normals(*plans[p]));
     if (bm) o << "#include \"ag_emu64_bm.cuh\"\n";
+    bool tf = false;
+    for (size_t p = 0; p < plans.size(); ++p) tf = tf || (lows[p].math == 3 && plans[p]->dst_dtype == DType::F64);
+    if (tf) o << "#include \"ag_tf64.cuh\"\n";
     o << "#define AG_BLOCK " << block << "\n#define AG_IPT " << ipt << "\n";
     std::vector<int> vecs;
     for (size_t p = 0; p < plans.size(); ++p) {

@@ -52,7 +52,7 @@ def make_workload(n_items, median, sigma, lo, hi, seed, math=0):
     return items
 
 
-@pytest.mark.parametrize("math", [0, 1])
+@pytest.mark.parametrize("math", [0, 1, 3])
 def test_batch_equals_per_item_launches_and_graph_replay(math):
     work = make_workload(300, 600, 1.5, 1, 40000, seed=3, math=math)
     launches = [ag.prepare(out, e, math=math) for out, e, _ in work]

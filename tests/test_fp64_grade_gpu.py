@@ -210,3 +210,25 @@ def test_scalars_and_literals_keep_their_bits():
     ag.assign(d, a.view() * ag.literal(np.pi), math=3)
     ref = (a.host().astype(np.longdouble) * np.longdouble(np.pi))
     assert np.max(np.abs(d.host() - ref) / np.spacing(np.abs(d.host()))) <= 0.5 + 1e-6
+
+
+def test_sum_and_accumulate():
+    """Sum plans reduce the FP64-grade terms with the same compensated tree;
+    += plans add them to the destination in FP64."""
+    n = 1 << 20
+    a = ag.Array("f64", (3,), n)
+    ag.assign(a, ag.Generator(23).uniform(3, -2.0, 2.0))
+    A = a.view()
+    s3 = ag.global_sum(A.dot(A) + ag.cwiseLog1p(ag.cwiseAbs(A)).sum(), n, math=3).cpu().numpy()
+    s0 = ag.global_sum(A.dot(A) + ag.cwiseLog1p(ag.cwiseAbs(A)).sum(), n, math=0).cpu().numpy()
+    assert abs((s3[0] + s3[1]) - (s0[0] + s0[1])) <= 1e-13 * abs(s0[0])
+    d3, d0 = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
+    ag.assign(d3, A * 0.5, math=0)
+    ag.assign(d0, A * 0.5, math=0)
+    e = ag.cwiseSqrt(ag.cwiseAbs(A)) + A * A
+    for _ in range(2):
+        ag.assign_add(d3, e, math=3)
+        ag.assign_add(d0, e, math=0)
+    H = a.host()
+    scale = np.abs(H) * 0.5 + 2 * (np.sqrt(np.abs(H)) + H * H)
+    assert_ulp(d3.host(), d0.host(), NATIVE_EXPR_ULPS, scale, "+= at FP64 grade")
