@@ -33,7 +33,8 @@ DEVICE_INC = os.path.join(REPO, "include", "aether", "gb300")
 EMBED = [("kAgDeviceSrc", "ag_device.cuh"), ("kAgEmu64Src", "ag_emu64.cuh"),
          ("kAgEmu64TablesSrc", "ag_emu64_tables.cuh"), ("kAgEmu64BmSrc", "ag_emu64_bm.cuh"),
          ("kAgEmu64BmTablesSrc", "ag_emu64_bm_tables.cuh"), ("kAgTf64Src", "ag_tf64.cuh"),
-         ("kAgTf64TablesSrc", "ag_tf64_tables.cuh")]
+         ("kAgTf64TablesSrc", "ag_tf64_tables.cuh"), ("kAgTf64TrigSrc", "ag_tf64_trig.cuh"),
+         ("kAgTf64TrigTablesSrc", "ag_tf64_trig_tables.cuh")]
 # The device-safe consumer headers (aether/device.h and what it includes),
 # exported with the engine's device runtime as the NVRTC payload for code
 # generators, each under its include name.

@@ -92,7 +92,8 @@ const Header kHeaders[] = {
     {"ag_device.cuh", kAgDeviceSrc},           {"ag_emu64.cuh", kAgEmu64Src},
     {"ag_emu64_tables.cuh", kAgEmu64TablesSrc}, {"ag_emu64_bm.cuh", kAgEmu64BmSrc},
     {"ag_emu64_bm_tables.cuh", kAgEmu64BmTablesSrc}, {"ag_tf64.cuh", kAgTf64Src},
-    {"ag_tf64_tables.cuh", kAgTf64TablesSrc},
+    {"ag_tf64_tables.cuh", kAgTf64TablesSrc}, {"ag_tf64_trig.cuh", kAgTf64TrigSrc},
+    {"ag_tf64_trig_tables.cuh", kAgTf64TrigTablesSrc},
 };
 constexpr int kNumHeaders = int(sizeof(kHeaders) / sizeof(kHeaders[0]));
 

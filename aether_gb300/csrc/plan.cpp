@@ -963,6 +963,14 @@ std::string kernel_base(const Plan& plan, const std::string& text) {
     return buf;
 }
 
+// FP64-grade plans with trigonometric nodes include the triple-float sine
+// and cosine (and their table).
+bool uses_trig(const Plan& P) {
+    for (const Node& n : P.nodes)
+        if (n.op == "sin" || n.op == "cos") return true;
+    return false;
+}
+
 // Plans with normal or lognormal leaves include the Box-Muller header when
 // lowered to double-float.
 bool draws_normals(const Plan& P) {
@@ -1018,6 +1026,7 @@ std::string generate_source(const Plan& plan_in, const Lowering& low, const std:
         o << "#include \"ag_device.cuh\"\n";
         if (low.math >= 1) o << "#include \"ag_emu64.cuh\"\n";
         if (tfx) o << "#include \"ag_tf64.cuh\"\n";
+        if (tfx && uses_trig(P)) o << "#include \"ag_tf64_trig.cuh\"\n";
         if (low.math >= 1 && draws_normals(P)) o << "#include \"ag_emu64_bm.cuh\"\n";
         o << "#define AG_BLOCK " << low.block << "\n#define AG_IPT " << low.ipt << "\n#define AG_VEC " << vec << "\n";
     }
@@ -1250,6 +1259,10 @@ std::string generate_batch_source(const std::vector<const Plan*>& plans, const s
     bool tf = false;
     for (size_t p = 0; p < plans.size(); ++p) tf = tf || (lows[p].math == 3 && plans[p]->dst_dtype == DType::F64);
     if (tf) o << "#include \"ag_tf64.cuh\"\n";
+    bool tft = false;
+    for (size_t p = 0; p < plans.size(); ++p)
+        tft = tft || (lows[p].math == 3 && plans[p]->dst_dtype == DType::F64 && uses_trig(*plans[p]));
+    if (tft) o << "#include \"ag_tf64_trig.cuh\"\n";
     o << "#define AG_BLOCK " << block << "\n#define AG_IPT " << ipt << "\n";
     std::vector<int> vecs;
     for (size_t p = 0; p < plans.size(); ++p) {

@@ -42,7 +42,7 @@ def _device_name():
 
 
 # Device headers only FP64-grade (math 3) kernels include.
-_TF_HEADERS = ("ag_tf64.cuh", "ag_tf64_tables.cuh")
+_TF_HEADERS = ("ag_tf64.cuh", "ag_tf64_tables.cuh", "ag_tf64_trig.cuh", "ag_tf64_trig_tables.cuh")
 
 
 def _code_digest(math=0):

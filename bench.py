@@ -291,7 +291,7 @@ def secondary_config1(ag):
     d = ag.Array("f64", (3,), n)
     e = a + b * c + ag.cwiseSin(a) * ag.cwiseExp((c * c) * (-1.0))
     out = {"samples": n, "bytes_per_sample": 96}
-    for name, m in (("native", 0), ("emulated", 1)):
+    for name, m in (("native", 0), ("emulated", 1), ("fp64_grade", 3)):
         L = ag.prepare(d, e, math=m, tune=True)
         ms = _time_ms(L, reps=20)
         out[name] = {"ms": round(ms, 4), "gbs": round(n * 96 / (ms * 1e-3) / 1e9, 1)}

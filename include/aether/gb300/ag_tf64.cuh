@@ -21,16 +21,19 @@
 // Range: inputs with magnitudes in [2^-40, 2^60] (and products the generator
 // cannot prove to stay above 2^-80) keep every component a normal float;
 // other lanes, non-finite or out-of-range outputs, and the functions without
-// a triple-float kernel here (exp, trig and the rest) are computed with
-// native FP64, so range and special values keep FP64 semantics.
+// a triple-float kernel (tan, the inverse trigonometric and hyperbolic
+// functions, pow and the rest) are computed with native FP64, so range and
+// special values keep FP64 semantics.
 //
 // Methods (published; own code): Knuth two-sum, Dekker Fast2Sum, FMA
 // two-product; Newton-Raphson square root, reciprocal square root and
 // reciprocal, each a double-float result from ag_emu64.cuh refined by one
 // step whose residual is formed exactly enough in triple-float; the
 // table-driven logarithm of Tang (1990) with the reduction points of the
-// double-float kernel and a third float on every table value
-// (gen_tf64_tables.py).
+// double-float kernel and a third float on every table value; the
+// table-driven exponential of Tang (1989); sine and cosine (ag_tf64_trig.cuh)
+// by a four-part Cody-Waite reduction by pi/2 and a table of sin and cos at
+// j/2048 (tables by gen_tf64_tables.py).
 #pragma once
 
 #include "ag_emu64.cuh"
@@ -349,11 +352,43 @@ template <bool U = false>
 __device__ __forceinline__ tf normal_df(ag_u64 seed, ag_u32 g, ag_u32 c) {
     return dfc(ag::normal_f64(seed, g, c));
 }
-// exp, sin and cos keep the double-float kernels' signature (a range flag
-// they leave alone here) and run on the native pipe.
-__device__ __forceinline__ tf exp_(tf a, bool&) { return dfc(ag::f_exp(as_d(a))); }
-__device__ __forceinline__ tf sin_(tf a, bool&) { return dfc(ag::f_sin(as_d(a))); }
-__device__ __forceinline__ tf cos_(tf a, bool&) { return dfc(ag::f_cos(as_d(a))); }
+// ---------------------------------------------------------------------------
+// exp: x = k ln2/64 + r, |r| <= ln2/128, e^x = 2^(k >> 6) T_(k & 63) (1 + p),
+// T_j = 2^(j/64) from a table of three floats, p = e^r - 1 = r + r^2 Q(r),
+// Q = 1/2 + r/6 + r^2/24 + r^3/120 + r^4/720 + r^5/5040 (the next term is
+// below 2^-66). r = x - k (ln2/64) with ln2/64 as three floats (k < 2^13, so
+// the product is good to 2^-63 absolute, the sum exact to 2^-64). r^2 Q is at
+// most 2^-16: formed in double-float (2^-46 of itself), with 1/6 and 1/24 as
+// float pairs where their products with r sit within 2^-12 of the terms
+// before them. The flag is cleared outside -55 < x < 87, where 2^(k >> 6) or
+// the result's third float would leave the normal floats (the native lane
+// computes those).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ tf exp_(tf x, bool& ok) {
+    ok = ok && x.x > -55.0f && x.x < 87.0f;
+    const float kx = __fmul_rn(x.x, AG_TF_INV_LN2_64);
+    const float kf = e64::rint_f(kx);
+    const int k = e64::rint_i(kx);
+    const tf r = renorm(sub(x, mul(mk3(AG_TF_LN2_64_X, AG_TF_LN2_64_Y, AG_TF_LN2_64_Z), kf)));
+    const df rr = mk(r.x, r.y);
+    const float rh = r.x;
+    const float J = __fmaf_rn(rh, __fmaf_rn(rh, 1.98412698e-4f, 1.38888889e-3f), 8.33333333e-3f);
+    const df H = e64::add_quick(mk(AG_TF_24TH_HI, AG_TF_24TH_LO), __fmul_rn(rh, J));
+    const df G = e64::add_quick(mk(AG_TF_SIXTH_HI, AG_TF_SIXTH_LO), e64::mul(rr, H));
+    const df Q = e64::add_quick(mk(0.5f, 0.0f), e64::mul(rr, G));
+    const df P = e64::mul(e64::sqr(rr), Q);
+    // p = r + P: |P| <= r^2 < |r|
+    const df h = fast_two_sum(r.x, P.hi);
+    const df m = two_sum(h.lo, r.y);
+    const tf p = mk3(h.hi, m.hi, __fadd_rn(__fadd_rn(m.lo, r.z), P.lo));
+    const e64::f4 tv = e64::ld4(kExp2Tab3, k & 63);
+    const tf T = mk3(tv.x, tv.y, tv.z);
+    // T >= 1 leads T p (|p| < 2^-7)
+    const tf res = add_lead(T, mul(T, p));
+    int e = k >> 6;
+    e = e < -126 ? -126 : (e > 126 ? 126 : e);
+    return scale(res, e64::p2f(e));
+}
 #define AG_T64_NATIVE1(NAME)                                                                   \
     __device__ __forceinline__ tf nat_##NAME(tf x) { return dfc(ag::f_##NAME(as_d(x))); }
 #define AG_T64_NATIVE2(NAME)                                                                   \

@@ -18,6 +18,7 @@ inline double normal_f64(ag_u64, ag_u32, ag_u32) { return std::nan(""); }
 }  // namespace ag
 
 #include "../../include/aether/gb300/ag_tf64.cuh"
+#include "../../include/aether/gb300/ag_tf64_trig.cuh"
 
 #include <cstdio>
 #include <random>
@@ -121,6 +122,56 @@ int main() {
          [](Q x) { return log1pq(x); });
     unop("log1p_neg", [&] { return -0.99 * u01(rng); }, [](tf x) { return log1p_(x); },
          [](Q x) { return log1pq(x); });
+
+    auto flagged = [&](const char* name, auto gen, auto f, auto ref) {
+        Stat s;
+        long native = 0;
+        for (int i = 0; i < N; ++i) {
+            const double x = gen();
+            bool ok = true;
+            const tf t = split(x, ok);
+            if (!ok) continue;
+            const tf r = f(t, ok);
+            if (!ok || !out_ok(r)) {   // lanes the generated kernel computes natively
+                ++native;
+                continue;
+            }
+            const Q exact = ref((Q)x);
+            s.add(val(r), exact, fabsq(exact));
+        }
+        s.bad += native > N / 1000 ? native : 0;   // more than 0.1 % native lanes is a failure
+        out.push_back({name, s});
+    };
+    flagged("exp", [&] { return -54.0 + 140.0 * u01(rng); }, [](tf x, bool& ok) { return exp_(x, ok); },
+            [](Q x) { return expq(x); });
+    flagged("exp_small", [&] { return sgn() * logu(-40, -1); }, [](tf x, bool& ok) { return exp_(x, ok); },
+            [](Q x) { return expq(x); });
+    flagged("sin", [&] { return sgn() * logu(-30, 9.99); }, [](tf x, bool& ok) { return sin_(x, ok); },
+            [](Q x) { return sinq(x); });
+    flagged("cos", [&] { return sgn() * logu(-30, 9.99); }, [](tf x, bool& ok) { return cos_(x, ok); },
+            [](Q x) { return cosq(x); });
+    flagged("sin_unit", [&] { return 2.0 * u01(rng) - 1.0; }, [](tf x, bool& ok) { return sin_(x, ok); },
+            [](Q x) { return sinq(x); });
+    {   // near nonzero multiples of pi/2: beyond 2^-22 of them every lane is kept
+        Stat s;
+        long native = 0;
+        const Q pio2 = acosq((Q)0);   // pi/2
+        for (int i = 0; i < N; ++i) {
+            const int q = 1 + (int)(u01(rng) * 600);
+            const double x = (double)(q * pio2) + sgn() * logu(-21, -3);
+            bool ok = true;
+            const tf t = split(x, ok);
+            const tf r = (i % 2) ? sin_(t, ok) : cos_(t, ok);
+            if (!ok) {
+                ++native;
+                continue;
+            }
+            const Q exact = (i % 2) ? sinq((Q)x) : cosq((Q)x);
+            s.add(val(r), exact, fabsq(exact));
+        }
+        s.bad += native;
+        out.push_back({"trig_near_multiples", s});
+    }
 
     {   // the large streaming expression, reassembled, in ulps of its term scale
         Stat s;

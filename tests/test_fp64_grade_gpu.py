@@ -96,6 +96,41 @@ def test_config1_against_reference(ref_cases):
     assert_ulp(d.host(), z["cfg1_d"], NATIVE_EXPR_ULPS, scale, "config 1 FP64-grade vs reference")
 
 
+def test_config1_full_size_against_exact(oracle):
+    """Config 1 at 2^20 samples: sin and exp in triple-float as well."""
+    n = 1 << 20
+    arrs = [ag.Array("f64", (3,), n) for _ in range(3)]
+    for k, arr in enumerate(arrs):
+        ag.assign(arr, ag.Generator(42).substream(k).uniform(3, -1.0, 1.0))
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, _cfg1(*(x.view() for x in arrs)), math=3)
+    A, B, C = (np.asarray(x.host(), dtype=np.longdouble) for x in arrs)
+    t3 = np.sin(A) * np.exp(-C * C)
+    exact = A + B * C + t3
+    scale = np.maximum.reduce([np.abs(A), np.abs(B * C), np.abs(t3)])
+    assert _ulps_of_scale(d.host(), exact, scale) <= FP64_GRADE_EXACT_ULPS
+    assert_ulp(d.host(), oracle.cfg1(*(x.host() for x in arrs)), NATIVE_EXPR_ULPS, scale.astype(np.float64),
+               "config 1 FP64-grade vs oracle")
+
+
+@pytest.mark.parametrize("fn", ["exp", "sin", "cos"])
+def test_functions_against_exact(fn):
+    """exp over (-50, 80), sin and cos over |x| < 1000 (the triple-float
+    ranges; lanes outside them or near nonzero multiples of pi/2 are native)."""
+    n = 1 << 16
+    x = ag.Array("f64", (1,), n)
+    lo, hi = (-50.0, 80.0) if fn == "exp" else (-1000.0, 1000.0)
+    ag.assign(x, ag.Generator(29).uniform(1, lo, hi))
+    X = x.view()
+    e = {"exp": ag.cwiseExp(X), "sin": ag.cwiseSin(X), "cos": ag.cwiseCos(X)}[fn]
+    d = ag.Array("f64", (1,), n)
+    ag.assign(d, e, math=3)
+    H = np.asarray(x.host(), dtype=np.longdouble)
+    exact = {"exp": np.exp, "sin": np.sin, "cos": np.cos}[fn](H)
+    err = np.abs(np.asarray(d.host(), dtype=np.longdouble) - exact) / np.spacing(np.abs(exact.astype(np.float64)))
+    assert float(err.max()) <= 1.0, (fn, float(err.max()))
+
+
 def _q(x):
     return np.asarray(x, dtype=np.longdouble)
 

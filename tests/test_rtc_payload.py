@@ -28,7 +28,7 @@ extern "C" __global__ void user_kernel(double* out, unsigned long long key, unsi
 
 
 RUNTIME = ["ag_device.cuh", "ag_emu64.cuh", "ag_emu64_tables.cuh", "ag_emu64_bm.cuh", "ag_emu64_bm_tables.cuh",
-           "ag_tf64.cuh", "ag_tf64_tables.cuh"]
+           "ag_tf64.cuh", "ag_tf64_tables.cuh", "ag_tf64_trig.cuh", "ag_tf64_trig_tables.cuh"]
 CONSUMER = ["aether/macros.h", "aether/detail/std.h", "aether/layout.h", "aether/math.h", "aether/expression.h",
             "aether/nodes.h", "aether/geometry.h", "aether/view.h", "aether/item.h", "aether/bundle.h", "aether/detail/philox.h",
             "aether/random.h", "aether/device.h"]

@@ -1,8 +1,8 @@
 """Host check of the FP64-grade triple-float kernels (ag_tf64.cuh) against
 113-bit arithmetic (tests/emu_host/tf_check.cpp, __float128): the split is
 exact and reassembles to the same double; sums, products, quotients, square
-roots, reciprocal square roots, logarithms and log1p stay within a small
-fraction of a double ulp; the large streaming expression
+roots, reciprocal square roots, logarithms, log1p, exp, sin and cos stay within
+a small fraction of a double ulp (sin and cos also near multiples of pi/2); the large streaming expression
 sqrt(a*a+b*b)*log1p(|c|) + rsqrt(1+d0*d0) rounds to within
 FP64_GRADE_EXACT_ULPS of its term scale."""
 
@@ -20,7 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # units of 2^-53 of the result (of the larger operand for sums)
 BOUNDS = {"split": 0.0, "add": 0.01, "sub": 0.01, "mul": 0.01, "div": 0.01, "sqr_then_mul": 0.01, "cancel": 0.01,
           "sqrt": 0.01, "rsqrt": 0.01, "recip": 0.01, "log": 0.25, "log_near_1": 0.25, "log1p": 0.25,
-          "log1p_nn": 0.25, "log1p_neg": 0.25}
+          "log1p_nn": 0.25, "log1p_neg": 0.25, "exp": 0.25, "exp_small": 0.25, "sin": 0.25, "cos": 0.25,
+          "sin_unit": 0.25, "trig_near_multiples": 0.5}
 
 
 @pytest.fixture(scope="module")
