@@ -36,9 +36,10 @@ EMU_EXPR_BOUND_2M53 = 512
 EMU_NORMAL_BOUND_2M53 = 256
 
 # FP64-grade lowering (math 3): doubles split exactly into three floats; sums,
-# products, quotients, sqrt, rsqrt, log and log1p in triple-float arithmetic
-# (each within about 2^-60 relative on the host check against 113-bit
-# arithmetic, tests/emu_host/tf_check.cpp), exp and trig on the native pipe;
+# products, quotients, sqrt, rsqrt, log, log1p, exp, sin and cos in
+# triple-float arithmetic (each within about 2^-60 relative on the host check
+# against 113-bit arithmetic, tests/emu_host/tf_check.cpp), the other
+# functions on the native pipe;
 # each output is the triple-float value rounded once to a double. Against
 # exact arithmetic: this many ulps of the term scale (measured 1.0 on the
 # host, the final rounding). Against the oracle (itself a few ulps from exact)

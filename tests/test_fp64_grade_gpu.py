@@ -56,7 +56,11 @@ def _cfg2a_exact(A, B, C, D0):
 
 
 def _ulps_of_scale(got, exact, scale):
-    sp = np.spacing(np.asarray(scale, dtype=np.float64))
+    """max |got - exact| in ulps of max(|exact|, term scale): the result's own
+    rounding is half an ulp of the result, which can exceed the term scale
+    when terms of one sign add up."""
+    mag = np.maximum(np.abs(np.asarray(exact, dtype=np.float64)), np.asarray(scale, dtype=np.float64))
+    sp = np.spacing(mag)
     return float(np.max(np.abs(np.asarray(got, dtype=np.longdouble) - exact) / sp.astype(np.longdouble)))
 
 
