@@ -16,7 +16,15 @@
 //     2^60], exp arguments outside (-70, 87), trig arguments beyond 2^24,
 //     special values) and results that would not reassemble exactly take
 //     CUDA's FP64 function instead, so range and special values keep FP64
-//     semantics.
+//     semantics;
+//   * one compiled with AETHER_GB300_FP64_GRADE defined evaluates the same
+//     functions in triple-float arithmetic on the FP32/INT pipes (aether/
+//     gb300/ag_tf64.cuh and ag_tf64_trig.cuh, the lowering of the engine's
+//     FP64-grade plans): within a small fraction of an ulp before the one
+//     rounding to double, the FP64 contract, with CUDA's FP64 function for
+//     |x| outside [2^-40, 2^60], exp arguments outside (-55, 87), trig
+//     arguments beyond 2^10 or near nonzero multiples of pi/2, and special
+//     values. The two macros exclude each other.
 // Every function is usable from device and host code.
 #pragma once
 
@@ -26,9 +34,18 @@
 
 #include "aether/macros.h"
 
+#if defined(AETHER_GB300_EMULATED_FP64) && defined(AETHER_GB300_FP64_GRADE)
+#error "aether/math.h: define at most one of AETHER_GB300_EMULATED_FP64 and AETHER_GB300_FP64_GRADE"
+#endif
 #if defined(__CUDACC__) && defined(AETHER_GB300_EMULATED_FP64)
 #include "aether/gb300/ag_device.cuh"
 #include "aether/gb300/ag_emu64.cuh"
+#endif
+// ag_tf64_trig.cuh brings ag_tf64.cuh and ag_emu64.cuh by their bare names
+// (one copy each under NVRTC, whose payload also names them by these paths)
+#if defined(__CUDACC__) && defined(AETHER_GB300_FP64_GRADE)
+#include "aether/gb300/ag_device.cuh"
+#include "aether/gb300/ag_tf64_trig.cuh"
 #endif
 
 namespace aether {
@@ -55,6 +72,29 @@ AETHER_GB300_EMU1(log1p, ::ag::e64::log1p_(v), ::log1p)
 AETHER_GB300_EMU1(sin, ::ag::e64::sin_(v, ok), ::sin)
 AETHER_GB300_EMU1(cos, ::ag::e64::cos_(v, ok), ::cos)
 #undef AETHER_GB300_EMU1
+}  // namespace emu
+#define AETHER_GB300_D(EMU, NATIVE) EMU
+#elif defined(__CUDA_ARCH__) && defined(AETHER_GB300_FP64_GRADE)
+namespace emu {
+// One triple-float evaluation of f at x, or CUDA's FP64 function where the
+// triple-float path cannot answer.
+#define AETHER_GB300_TF1(NAME, BODY, NATIVE)                                   \
+    __device__ inline double NAME(double x) {                                  \
+        bool ok = true;                                                        \
+        const ::ag::t64::tf v = ::ag::t64::from_double_ck(x, ok);              \
+        const ::ag::t64::tf r = BODY;                                          \
+        const double y = ::ag::t64::to_double(r);                              \
+        return (ok && ::ag::t64::out_ok(r) && y == y) ? y : NATIVE(x);         \
+    }
+__device__ inline double native_rsqrt(double x) { return __ddiv_rn(1.0, __dsqrt_rn(x)); }
+AETHER_GB300_TF1(sqrt, ::ag::t64::sqrt_(v), __dsqrt_rn)
+AETHER_GB300_TF1(rsqrt, ::ag::t64::rsqrt_(v), native_rsqrt)
+AETHER_GB300_TF1(exp, ::ag::t64::exp_(v, ok), ::exp)
+AETHER_GB300_TF1(log, ::ag::t64::log_(v), ::log)
+AETHER_GB300_TF1(log1p, ::ag::t64::log1p_(v), ::log1p)
+AETHER_GB300_TF1(sin, ::ag::t64::sin_(v, ok), ::sin)
+AETHER_GB300_TF1(cos, ::ag::t64::cos_(v, ok), ::cos)
+#undef AETHER_GB300_TF1
 }  // namespace emu
 #define AETHER_GB300_D(EMU, NATIVE) EMU
 #else

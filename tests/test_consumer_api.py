@@ -9,7 +9,8 @@ reference consumer uses it, checked against the oracle.
   spelling (tests/test_GraphCapture.cu:45-58 is the idiom) compiled unmodified
   by nvcc against -I include: Philox fills bit-exact, arithmetic and geometry
   bit-exact with --fmad=false, transcendental expressions within the native
-  bound of aether_gb300.accuracy, and the emulated-FP64 math facade within its
+  bound of aether_gb300.accuracy (also with the FP64-grade math facade,
+  AETHER_GB300_FP64_GRADE), and the emulated-FP64 math facade within its
   bound.
 """
 
@@ -134,6 +135,7 @@ def test_consumer_kernels_compile_for_sm103a(tmp_path):
     _nvcc_build(tmp_path, "ck_default", [])
     _nvcc_build(tmp_path, "ck_exact", ["--fmad=false"])
     _nvcc_build(tmp_path, "ck_emulated", ["-DAETHER_GB300_EMULATED_FP64"])
+    _nvcc_build(tmp_path, "ck_fp64_grade", ["-DAETHER_GB300_FP64_GRADE"])
 
 
 def _run_kernels(tmp_path, exe, n):
@@ -152,12 +154,13 @@ def _run_kernels(tmp_path, exe, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", ["default", "exact", "emulated"])
+@pytest.mark.parametrize("variant", ["default", "exact", "emulated", "fp64_grade"])
 def test_consumer_kernels_on_device(tmp_path, oracle, variant):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    extra = {"default": [], "exact": ["--fmad=false"], "emulated": ["-DAETHER_GB300_EMULATED_FP64"]}[variant]
+    extra = {"default": [], "exact": ["--fmad=false"], "emulated": ["-DAETHER_GB300_EMULATED_FP64"],
+             "fp64_grade": ["-DAETHER_GB300_FP64_GRADE"]}[variant]
     exe = _nvcc_build(tmp_path, "ck_" + variant, extra)
     n = 4099
     res = _run_kernels(tmp_path, exe, n)

@@ -63,7 +63,7 @@ def test_payload_headers_and_digest():
 
 
 def test_device_h_kernel_compiles_with_nvrtc():
-    for opts in ([], ["-DAETHER_GB300_EMULATED_FP64"], ["--fmad=false"]):
+    for opts in ([], ["-DAETHER_GB300_EMULATED_FP64"], ["-DAETHER_GB300_FP64_GRADE"], ["--fmad=false"]):
         cubin = rtc.compile(DEVICE_H_KERNEL, options=opts)
         assert len(cubin) > 1000 and cubin[:4] == b"\x7fELF"
     with pytest.raises(Exception, match="NVRTC"):
