@@ -271,3 +271,33 @@ def test_sum_and_accumulate():
     H = a.host()
     scale = np.abs(H) * 0.5 + 2 * (np.sqrt(np.abs(H)) + H * H)
     assert_ulp(d3.host(), d0.host(), NATIVE_EXPR_ULPS, scale, "+= at FP64 grade")
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 37, 255, 257, 513, 1025, 4099])
+def test_ragged_sizes_and_tails(n):
+    """Lane groups, chunk tails and single samples at FP64 grade: the
+    deferred native recomputation and the stores stop at n."""
+    arrs = [ag.Array("f64", (3,), n) for _ in range(4)]
+    for k, arr in enumerate(arrs):
+        ag.assign(arr, ag.Generator(40 + k).uniform(3, -4.0, 4.0))
+    d = ag.Array("f64", (3,), n)
+    d.data.fill_(7.0)
+    ag.assign(d, _cfg2a(*(x.view() for x in arrs)), math=3)
+    exact, scale = _cfg2a_exact(*(x.host() for x in arrs))
+    assert _ulps_of_scale(d.host(), exact, scale) <= FP64_GRADE_EXACT_ULPS
+    # capacity padding past n is left alone
+    if d.data.shape[1] > n:
+        assert bool((d.data[:, n:] == 7.0).all())
+
+
+def test_misaligned_operands_take_the_scalar_kernel():
+    n = 1001
+    base = torch.zeros((3, 1100), dtype=torch.float64, device="cuda")
+    a = ag.Array("f64", (3,), n)
+    ag.assign(a, ag.Generator(5).uniform(3, -1.0, 1.0))
+    base[:, 1:1 + n] = a.data[:, :n]
+    mis = ag.expr.Operand(base.data_ptr() + 8, 1100, "f64", (3,))   # planes 8 bytes past 16
+    d1, d2 = ag.Array("f64", (3,), n), ag.Array("f64", (3,), n)
+    ag.assign(d1, ag.cwiseExp(a.view()) * ag.cwiseSqrt(a.view() * a.view() + 1.0), math=3)
+    ag.assign(d2, ag.cwiseExp(mis) * ag.cwiseSqrt(mis * mis + 1.0), math=3)
+    assert np.array_equal(d1.host(), d2.host())
