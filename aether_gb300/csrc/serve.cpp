@@ -9,14 +9,17 @@
 // the slots' completion events and retires their requests. Submitting threads
 // only append to the queue.
 //
-// A launch slot is a stream, a work-list buffer and its pinned staging, and two
-// events. A slot is reused only after its completion event has fired, so its
-// staging, its work list and the arena bytes its requests freed are no longer
-// read by the device when they are written again.
+// A launch slot is a stream, a work-list buffer and its pinned staging, and
+// checkpoint events: one after each plan's run (its kernel and its requests'
+// output copies), so a request retires -- and frees its arena bytes -- as soon
+// as its own run has finished, not when the whole launch has. A slot is reused
+// only after its last checkpoint has fired, so its staging and its work list
+// are no longer read by the device when they are written again.
 
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdint>
 #include <cstring>
 #include <deque>
 #include <list>
@@ -144,24 +147,32 @@ struct Upload {
 
 struct Slot {
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr, copied = nullptr, done_first = nullptr;
+    cudaEvent_t copied = nullptr;
     AgItemHost* staging = nullptr;
     void* dev_items = nullptr;
     std::vector<Request*> rs;         // the slot's requests (stable: the request deque only grows)
     // When some requests read only resident operands and others wait for
     // copies, the first n_first of rs run in a launch of their own that does
-    // not wait, and finish (done_first) before the rest.
+    // not wait for them.
     size_t n_first = 0;
-    bool first_retired = false;
+    // Checkpoints in stream order: after each run of one plan (its kernel and
+    // its requests' output copies) an event; requests [previous end, cp_end[k])
+    // retire when event k completes, so a request does not wait for the
+    // other plans of its launch.
+    std::vector<cudaEvent_t> cp_ev;   // created on first need, reused
+    std::vector<size_t> cp_end;
+    size_t cp_next = 0;               // the first checkpoint not yet seen complete
+    size_t retired = 0;               // requests of rs retired so far
     uint64_t upload_seq = 0;
     bool busy = false;
 };
 
-// A completion seen by the loop: part 1 = the slot's first group, 2 = all.
+// A completion seen by the loop: checkpoint `cp` of slot `s`, or the rest of
+// the slot (cp = SIZE_MAX) when an error ends it.
 struct Fin {
     Slot* s;
     cudaError_t e;
-    int part;
+    size_t cp;
 };
 
 struct Server {
@@ -330,22 +341,41 @@ struct Server {
             }
         }
         if (gb.n) ag_ck(ag_gather_copy(gb, sms, copy_stream), "gather copy");
-        if (!ups.empty() || wait_uploads) {
-            ag_ck(cudaEventRecord(S.copied, copy_stream), "cudaEventRecord(copied)");
-            ag_ck(cudaStreamWaitEvent(S.stream, S.copied, 0), "cudaStreamWaitEvent(copied)");
-        }
         const bool need_wait = !ups.empty() || wait_uploads;
         if (!need_wait) S.n_first = 0;
-        if (S.n_first) {
-            launch_group(S, 0, S.n_first);
-            ag_ck(cudaEventRecord(S.done_first, S.stream), "cudaEventRecord(done_first)");
-        }
+        S.cp_end.clear();
+        S.cp_next = 0;
+        S.retired = 0;
+        // requests on resident operands only: launched before the wait
+        if (S.n_first) launch_group(S, 0, S.n_first);
         if (need_wait) {
             ag_ck(cudaEventRecord(S.copied, copy_stream), "cudaEventRecord(copied)");
             ag_ck(cudaStreamWaitEvent(S.stream, S.copied, 0), "cudaStreamWaitEvent(copied)");
         }
         launch_group(S, S.n_first, S.rs.size() - S.n_first);
-        ag_ck(cudaEventRecord(S.done, S.stream), "cudaEventRecord(done)");
+    }
+
+    // Mark on the slot's stream the end of requests [.., end): they retire
+    // when this event completes.
+    void checkpoint(Slot& S, size_t end) {
+        const size_t k = S.cp_end.size();
+        if (k == S.cp_ev.size()) {
+            cudaEvent_t e = nullptr;
+            ag_ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate(checkpoint)");
+            S.cp_ev.push_back(e);
+        }
+        ag_ck(cudaEventRecord(S.cp_ev[k], S.stream), "cudaEventRecord(checkpoint)");
+        S.cp_end.push_back(end);
+    }
+
+    // The host output copies of requests [b, e) of a slot.
+    void copy_outputs(Slot& S, size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            const Request& r = *S.rs[i];
+            if (r.host_out)
+                ag_ck(cudaMemcpyAsync(r.host_out, base + r.out_off, r.out_bytes, cudaMemcpyDeviceToHost, S.stream),
+                      "cudaMemcpyAsync(output)");
+        }
     }
 
     // Launch requests [first, first + count) of a slot on its stream, then
@@ -372,6 +402,8 @@ struct Server {
         std::vector<AetherOperand> ops;
         if (count == 1) {
             launch_plain(*S.rs[first], S.stream, ops);
+            copy_outputs(S, first, first + 1);
+            checkpoint(S, first + 1);
         } else if (!plan_batch.empty()) {
             // grouped by plan (the caller sorted the range): one work list,
             // copied once, and one launch per plan -- its own kernel for a
@@ -418,6 +450,9 @@ struct Server {
                                            dim3(unsigned(B.block)), params, 0, S.stream),
                           "cudaLaunchKernel(batch)");
                 }
+                // this plan's requests finish here, before the runs after it
+                copy_outputs(S, first + b, first + e);
+                checkpoint(S, first + e);
                 b = e;
             }
         } else {
@@ -443,12 +478,8 @@ struct Server {
             ag_ck(cudaLaunchKernel(reinterpret_cast<const void*>(batch->kernel), dim3(batch_grid(*batch, tiles)),
                                    dim3(unsigned(batch->block)), params, 0, S.stream),
                   "cudaLaunchKernel(batch)");
-        }
-        for (size_t i = 0; i < count; ++i) {
-            const Request& r = *S.rs[first + i];
-            if (r.host_out)
-                ag_ck(cudaMemcpyAsync(r.host_out, base + r.out_off, r.out_bytes, cudaMemcpyDeviceToHost, S.stream),
-                      "cudaMemcpyAsync(output)");
+            copy_outputs(S, first, first + count);
+            checkpoint(S, first + count);
         }
     }
 
@@ -479,16 +510,16 @@ struct Server {
     void retire(const std::vector<Fin>& fin, uint64_t t) {
         for (const Fin& f : fin) {
             Slot& S = *f.s;
-            if (f.part == 1) {
-                retire_range(S, 0, S.n_first, f.e, t);
-                S.first_retired = true;
-                continue;
-            }
-            retire_range(S, S.first_retired ? S.n_first : 0, S.rs.size(), f.e, t);
+            const size_t end = f.cp == SIZE_MAX ? S.rs.size() : S.cp_end[f.cp];
+            retire_range(S, S.retired, end, f.e, t);
+            S.retired = end;
+            if (S.retired < S.rs.size()) continue;
             uploads_done_seq = std::max(uploads_done_seq, S.upload_seq);
             S.rs.clear();
             S.n_first = 0;
-            S.first_retired = false;
+            S.cp_end.clear();
+            S.cp_next = 0;
+            S.retired = 0;
             S.busy = false;
         }
         if (!fin.empty()) cv_done.notify_all();
@@ -529,19 +560,19 @@ struct Server {
             fin.clear();
             for (Slot& S : slots) {
                 if (!S.busy) continue;
-                if (S.n_first && !S.first_retired) {
-                    const cudaError_t e1 = cudaEventQuery(S.done_first);
-                    if (e1 != cudaErrorNotReady) {
-                        if (e1 != cudaSuccess) cudaGetLastError();
-                        fin.push_back(Fin{&S, e1, 1});
+                // checkpoints complete in stream order
+                while (S.cp_next < S.cp_end.size()) {
+                    const cudaError_t e = cudaEventQuery(S.cp_ev[S.cp_next]);
+                    if (e == cudaErrorNotReady) break;
+                    if (e != cudaSuccess) {
+                        cudaGetLastError();
+                        fin.push_back(Fin{&S, e, SIZE_MAX});   // the rest of the slot fails
+                        S.cp_next = S.cp_end.size();
+                        break;
                     }
+                    fin.push_back(Fin{&S, e, S.cp_next});
+                    ++S.cp_next;
                 }
-                const cudaError_t e = cudaEventQuery(S.done);
-                if (e == cudaErrorNotReady) continue;
-                if (e != cudaSuccess) cudaGetLastError();
-                if (S.n_first && !S.first_retired && (fin.empty() || fin.back().s != &S))
-                    fin.push_back(Fin{&S, e, 1});   // the first group finished before the rest
-                fin.push_back(Fin{&S, e, 2});
             }
             const uint64_t t_fin = fin.empty() ? 0 : now();
             lk.lock();
@@ -573,12 +604,21 @@ struct Server {
                     const size_t ready = size_t(mid - S->rs.begin());
                     S->n_first = (ready > 0 && ready < S->rs.size()) ? ready : 0;
                     if (!plan_batch.empty()) {
-                        // each launch group ordered by plan: one run per plan
-                        auto by_plan = [](const Request* x, const Request* y) { return x->plan < y->plan; };
-                        std::stable_sort(S->rs.begin(), mid, by_plan);
-                        std::stable_sort(mid, S->rs.end(), by_plan);
+                        // each launch group ordered by plan, one run per plan,
+                        // the plan with the least work first: its requests
+                        // retire at their own checkpoint, before larger runs
+                        std::vector<uint64_t> work(plans.size());
+                        auto order = [&](std::vector<Request*>::iterator b, std::vector<Request*>::iterator e) {
+                            std::fill(work.begin(), work.end(), 0);
+                            for (auto it = b; it != e; ++it) work[size_t((*it)->plan)] += (*it)->n;
+                            std::stable_sort(b, e, [&](const Request* x, const Request* y) {
+                                const uint64_t wx = work[size_t(x->plan)], wy = work[size_t(y->plan)];
+                                return wx != wy ? wx < wy : x->plan < y->plan;
+                            });
+                        };
+                        order(S->rs.begin(), mid);
+                        order(mid, S->rs.end());
                     }
-                    S->first_retired = false;
                     S->busy = true;
                     // The completion of a slot that waited for the copy stream
                     // proves every copy enqueued before its wait has landed.
@@ -617,7 +657,9 @@ struct Server {
                         }
                         S->rs.clear();
                         S->n_first = 0;
-                        S->first_retired = false;
+                        S->cp_end.clear();
+                        S->cp_next = 0;
+                        S->retired = 0;
                         S->busy = false;
                         cv_done.notify_all();
                     }
@@ -773,9 +815,8 @@ void destroy(Server* S) {
     cudaSetDevice(S->dev);
     for (Slot& sl : S->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
-        if (sl.done) cudaEventDestroy(sl.done);
+        for (cudaEvent_t e : sl.cp_ev) cudaEventDestroy(e);
         if (sl.copied) cudaEventDestroy(sl.copied);
-        if (sl.done_first) cudaEventDestroy(sl.done_first);
         if (sl.staging) cudaFreeHost(sl.staging);
         if (sl.dev_items) cudaFree(sl.dev_items);
         if (sl.stream) cudaStreamDestroy(sl.stream);
@@ -852,9 +893,7 @@ AG_EXPORT int aether_serve_open(void* const* plans, int n_plans, const AetherSer
         const size_t items = S->cfg.mode == AETHER_SERVE_PLAIN ? 1 : size_t(S->cfg.max_items);
         for (Slot& sl : S->slots) {
             ag_ck(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking), "cudaStreamCreate(slot)");
-            ag_ck(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming), "cudaEventCreate");
             ag_ck(cudaEventCreateWithFlags(&sl.copied, cudaEventDisableTiming), "cudaEventCreate");
-            ag_ck(cudaEventCreateWithFlags(&sl.done_first, cudaEventDisableTiming), "cudaEventCreate");
             void* h = nullptr;
             ag_ck(cudaMallocHost(&h, items * sizeof(AgItemHost)), "cudaMallocHost(work list)");
             sl.staging = static_cast<AgItemHost*>(h);
