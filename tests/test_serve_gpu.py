@@ -173,3 +173,31 @@ def test_refusals_and_kept_outputs(shapes, pools):
         # an id that is resident needs no host bytes
         again = srv.request(cross, 1000, [7, 8], [0, 0])
         assert srv.wait(srv.submit(again))["uploaded_bytes"] == 0
+
+
+def test_fp64_grade_shapes(pools):
+    """Served shapes lowered at FP64 grade (math = 3): each request the same
+    alone, in a mix (per-plan work-list kernels of triple-float plans) and in
+    plain mode; the large streaming expression within 2 ulp of exact."""
+    base = {s.name: s for s in serve.standard_shapes()}
+    tf = [serve.ShapeTemplate(name + "_tf", "f64", base[name].out_shape, base[name].operands, base[name].build, math=3)
+          for name in ("expr1_f64", "expr2_f64", "cross_f64", "inv3_f64")]
+    trace = _trace(tf, 80, seed=8, reuse=0.5)
+    alone = _alone(tf, pools, trace)
+    mixed, sts, _ = _mixed(tf, pools, trace, max_items=32)
+    assert max(s["launch_items"] for s in sts) > 1
+    for a, m in zip(alone, mixed):
+        assert torch.equal(a, m)
+    plain, _, _ = _mixed(tf, pools, trace, mode="plain")
+    for a, p in zip(alone, plain):
+        assert torch.equal(a, p)
+    names = [s.name for s in tf]
+    n = 2049
+    out = _alone(tf, pools, [(names.index("expr2_f64_tf"), n, [701, 702, 703, 704], 0)])[0].numpy()
+    A, B, C, D0 = (np.asarray(pools.array("f64", i, 3, n), dtype=np.longdouble) for i in (701, 702, 703, 704))
+    t1 = np.sqrt(A * A + B * B) * np.log1p(np.abs(C))
+    t2 = 1 / np.sqrt(1 + D0 * D0)
+    exact = t1 + t2
+    mag = np.maximum(np.abs(exact), np.maximum(np.abs(t1), np.abs(t2))).astype(np.float64)
+    err = np.abs(np.asarray(out, dtype=np.longdouble) - exact) / np.spacing(mag)
+    assert float(err.max()) <= 2.0
