@@ -304,6 +304,12 @@ class Launch:
 def prepare(dst, expr, op="set", n=None, sample_offset=0, reduce_out=None, workspace=None, tune=False, **low):
     """Lower `dst <op>= expr` and bind its arguments; returns a Launch.
 
+    Lowering keywords (include/aether_gb300.h AetherLowering): math = 0 FP64
+    on the FP64 pipe, 1 double-float FP64 emulation (about 48 bits), 2 the
+    precision form (f32/ff storage, float-float arithmetic), 3 FP64-grade
+    triple-float on the FP32/INT pipes (f64 plans, the FP64 contract);
+    contract (FMA contraction), block, ipt, vec, min_blocks.
+
     tune=True takes the autotuned lowering of this plan on this device (see
     tune.py), timing the candidates first if none is cached. Only plans that
     overwrite their destination are tuned (set/sum/setsum)."""
