@@ -557,11 +557,16 @@ def time_steps(k_expr, k_fill, steps, stream):
     return (start.elapsed_time(end), [e[0].elapsed_time(e[1]) for e in ev], [e[1].elapsed_time(e[2]) for e in ev])
 
 
-def l2_twin_gbs(launch, samples, bytes_per_sample, reps=40):
+def l2_twin_gbs(launch, samples, bytes_per_sample, reps=40, min_ms=0.1):
     """The same kernel on an L2-resident slice (its working set well inside
     the 129 MB L2), back to back: the rate the kernel reaches when HBM is not
-    what limits it, i.e. its compute ceiling, in the same algorithmic bytes."""
+    what limits it, i.e. its compute ceiling, in the same algorithmic bytes.
+    None when one launch on the slice runs under min_ms: its ramp-up and tail
+    would then weigh more than its compute, and the rate would understate the
+    ceiling (the fast lowerings of the expression at 2^19 samples)."""
     ms = _time_ms(launch, reps=reps, warmup=3)
+    if ms < min_ms:
+        return None
     return samples * bytes_per_sample / (ms * 1e-3) / 1e9
 
 
@@ -814,7 +819,8 @@ def run_ours(args):
                 "issue_roof": "profiled thread instructions per sample (profiles/ncu_traffic.txt) at SMs x 4 "
                               "schedulers x 32 lanes x the sampled SM clock; l2_resident_gbs: the memory-free "
                               "twin, the same kernel timed on a slice that stays in L2 (2^23 fill doubles, 2^19 "
-                              "expression samples): its compute ceiling in the same algorithmic bytes"}
+                              "expression samples): its compute ceiling in the same algorithmic bytes, reported "
+                              "when one launch on the slice runs 0.1 ms or more"}
     cpu = None
     ref = None
     if not args.no_cpu:
