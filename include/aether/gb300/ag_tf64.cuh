@@ -223,8 +223,9 @@ __device__ __forceinline__ tf dfc(double v) {
     const float y = __double2float_rn(r);
     return mk3(x, y, __double2float_rn(r - (double)y));
 }
-// y + z is exact in a double for the overlaps the operations leave, so the
-// result is x + y + z rounded once.
+// y + z in a double is exact whenever their exponents lie within 29 of each
+// other, and otherwise off by at most 2^-53 of y (about 2^-77 of x): the
+// result is x + y + z rounded once, to far below half an ulp.
 __device__ __forceinline__ double to_double(tf v) {
     return __dadd_rn((double)v.x, __dadd_rn((double)v.y, (double)v.z));
 }
