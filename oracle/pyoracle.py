@@ -139,23 +139,27 @@ def fill_uniform_f32(key, lo, hi, comps, n, pitch=None, nthreads=0):
     return out
 
 
-def fill_normal_f64(key, mean, sd, comps, n, pitch=None, sample_offset=0, nthreads=0):
+def fill_normal_f64(key, mean, sd, comps, n, pitch=None, sample_offset=0, nthreads=0, out=None):
     pitch = pitch or n
-    out = np.zeros((comps, pitch), dtype=np.float64)
+    if out is None:
+        out = np.zeros((comps, pitch), dtype=np.float64)
+    assert out.dtype == np.float64 and out.flags.c_contiguous and out.shape == (comps, pitch)
     lib().orc_fill_normal_f64(key, mean, sd, comps, n, pitch, _ptr(out), sample_offset, nthreads)
     return out
 
 
-def cfg1(a, b, c, nthreads=0):
+def cfg1(a, b, c, nthreads=0, out=None):
     n = a.shape[1]
-    d = np.zeros_like(a)
+    d = np.zeros_like(a) if out is None else out
+    assert d.shape == a.shape and d.dtype == np.float64 and d.flags.c_contiguous
     lib().orc_cfg1_f64(_ptr(a), _ptr(b), _ptr(c), _ptr(d), n, n, nthreads)
     return d
 
 
-def cfg2a(a, b, c, d0, nthreads=0):
+def cfg2a(a, b, c, d0, nthreads=0, out=None):
     n = a.shape[1]
-    d = np.zeros_like(a)
+    d = np.zeros_like(a) if out is None else out
+    assert d.shape == a.shape and d.dtype == np.float64 and d.flags.c_contiguous
     lib().orc_cfg2a_f64(_ptr(a), _ptr(b), _ptr(c), _ptr(d0), _ptr(d), n, n, nthreads)
     return d
 

@@ -8,11 +8,17 @@
 // iteration with `dst[i] = expr`.
 //
 // usage: aether_ref <out_dir>     (prints a JSON manifest on stdout)
+//        aether_ref --bench [steps] (times the CPU arm's sample through the
+//                                    reference's headers, one JSON line)
 
 #include <aether/aether.h>
 
+#include <omp.h>
+
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -47,8 +53,50 @@ static void fill(aether::Array<T, N>& a, const Leaf& leaf) {
     for (std::size_t k = 0; k < a.samples(); ++k) v[SampleIndex::make(k)] = leaf;
 }
 
+// The CPU arm's sample timed through the reference's own headers: config 2a
+// on 2^23 samples and the N(0, 1) fill of 2^25 doubles, inputs from
+// Generator(7), each an OpenMP loop over SampleIndex::make(k) assigning
+// `view[i] = expr` (the user loop, tests/test_Random_common.h:63-70), as the
+// oracle's restatement runs them; prints the median of `steps` steps as JSON.
+static int bench(int steps) {
+    const std::size_t n = std::size_t(1) << 23, nf = std::size_t(1) << 25;
+    Generator g(7);
+    aether::Array<double, 3> a(n), b(n), c(n), d0(n), d(n);
+    aether::Array<double, 1> z(nf);
+    aether::Array<double, 3>* in[4] = {&a, &b, &c, &d0};
+    for (int s = 0; s < 4; ++s) {
+        auto v = in[s]->hostView();
+        const auto leaf = g.substream(std::uint64_t(s)).uniform<double, 3>(-4.0, 4.0);
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < long(n); ++k) v[SampleIndex::make(std::size_t(k))] = leaf;
+    }
+    auto av = a.hostView(), bv = b.hostView(), cv = c.hostView(), d0v = d0.hostView(), dv = d.hostView();
+    auto zv = z.hostView();
+    const auto normal = g.substream(4).normal<double, 1>(0.0, 1.0);
+    std::vector<double> ts;
+    for (int it = 0; it < steps + 1; ++it) {
+        const double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < long(n); ++k) {
+            aether::Item<double, 3> L;
+            for (std::size_t q = 0; q < 3; ++q) L(q) = aether::math::log1p(aether::math::abs(cv(q, std::size_t(k))));
+            dv[SampleIndex::make(std::size_t(k))] = aether::cwiseSqrt(av * av + bv * bv) * L +
+                                                     aether::cwiseRsqrt(aether::constant<aether::extents<3>>(1.0) + d0v * d0v);
+        }
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < long(nf); ++k) zv[SampleIndex::make(std::size_t(k))] = normal;
+        if (it) ts.push_back(omp_get_wtime() - t0);
+    }
+    std::sort(ts.begin(), ts.end());
+    const double t = ts[ts.size() / 2];
+    std::printf("{\"threads\": %d, \"s_per_step\": %.6f, \"gbs\": %.4f}\n", omp_get_max_threads(), t,
+                (double(n) * 120 + double(nf) * 8) / t / 1e9);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) return 2;
+    if (std::string(argv[1]) == "--bench") return bench(argc > 2 ? std::atoi(argv[2]) : 5);
     g_dir = argv[1];
     std::printf("[\n");
 
