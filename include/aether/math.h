@@ -25,6 +25,11 @@
 //     |x| outside [2^-40, 2^60], exp arguments outside (-55, 87), trig
 //     arguments beyond 2^10 or near nonzero multiples of pi/2, and special
 //     values. The two macros exclude each other.
+// The set is the reference's (math/math.h:20-32): the exponential, logarithmic,
+// root, trigonometric, hyperbolic and inverse functions, erf and erfc, the
+// rounding family (round half away from zero, rint half to even), fmod, fdim,
+// numpy's floored remainder, copysign, min/max/fmin/fmax, sign, clip, fma,
+// sincos and the classification predicates.
 // Every function is usable from device and host code.
 #pragma once
 
@@ -151,6 +156,26 @@ AETHER_MATH1(abs, ::fabs, ::fabsf, std::fabs)
 AETHER_MATH1(floor, ::floor, ::floorf, std::floor)
 AETHER_MATH1(ceil, ::ceil, ::ceilf, std::ceil)
 AETHER_MATH1(trunc, ::trunc, ::truncf, std::trunc)
+AETHER_MATH1(round, ::round, ::roundf, std::round)   // half away from zero
+AETHER_MATH1(rint, ::rint, ::rintf, std::rint)       // half to even
+AETHER_MATH1(asinh, ::asinh, ::asinhf, std::asinh)
+AETHER_MATH1(acosh, ::acosh, ::acoshf, std::acosh)
+AETHER_MATH1(atanh, ::atanh, ::atanhf, std::atanh)
+AETHER_MATH1(erfc, ::erfc, ::erfcf, std::erfc)
+#if !defined(__CUDACC_RTC__)
+namespace host {
+// 10^x: glibc's exp10 where the C library has one, else pow(10, x)
+template <class T>
+inline T exp10(T x) {
+#if defined(__GLIBC__)
+    return ::exp10(x);
+#else
+    return std::pow(T(10), x);
+#endif
+}
+}  // namespace host
+#endif
+AETHER_MATH1(exp10, ::exp10, ::exp10f, host::exp10)
 #undef AETHER_MATH1
 #undef AETHER_GB300_D
 
@@ -169,7 +194,31 @@ AETHER_MATH2(atan2, ::atan2, ::atan2f, std::atan2)
 AETHER_MATH2(hypot, ::hypot, ::hypotf, std::hypot)
 AETHER_MATH2(min, ::fmin, ::fminf, std::fmin)
 AETHER_MATH2(max, ::fmax, ::fmaxf, std::fmax)
+AETHER_MATH2(fmin, ::fmin, ::fminf, std::fmin)
+AETHER_MATH2(fmax, ::fmax, ::fmaxf, std::fmax)
+AETHER_MATH2(fmod, ::fmod, ::fmodf, std::fmod)        // sign of the dividend
+AETHER_MATH2(fdim, ::fdim, ::fdimf, std::fdim)
+AETHER_MATH2(copysign, ::copysign, ::copysignf, std::copysign)
 #undef AETHER_MATH2
+
+// -- sign, clip, remainder and the classification predicates ----------------
+// The reference's semantics (math/math.h:155-215, math/round.h:94-115): sign
+// is 0 for either zero and for NaN; clip lets NaN through and clamps the rest
+// to [lo, hi]; remainder is the floored remainder of numpy (the result takes
+// the divisor's sign, an exact zero takes it too), not C's IEEE remainder.
+template <class T>
+AETHER_DEVICEANDHOST() inline T clip(T x, T lo, T hi) {
+    const bool nan = x != x;
+    const T t = (nan || x >= lo) ? x : lo;
+    return (nan || t <= hi) ? t : hi;
+}
+template <class T>
+AETHER_DEVICEANDHOST() inline T remainder(T a, T b) {
+    T m = fmod(a, b);
+    if (m == T(0)) return copysign(T(0), b);
+    return ((m < T(0)) != (b < T(0))) ? m + b : m;
+}
+
 
 AETHER_DEVICEANDHOST() inline double fma(double a, double b, double c) {
 #if defined(__CUDA_ARCH__)
@@ -206,6 +255,18 @@ AETHER_DEVICEANDHOST() inline bool isfinite(float x) {
     return std::isfinite(x);
 #endif
 }
+#if defined(__CUDA_ARCH__)
+#define AETHER_MATH_PRED(NAME)                                                      \
+    AETHER_DEVICEANDHOST() inline bool NAME(double x) { return ::NAME(x); }          \
+    AETHER_DEVICEANDHOST() inline bool NAME(float x) { return ::NAME(x); }
+#else
+#define AETHER_MATH_PRED(NAME)                                                      \
+    AETHER_DEVICEANDHOST() inline bool NAME(double x) { return std::NAME(x); }       \
+    AETHER_DEVICEANDHOST() inline bool NAME(float x) { return std::NAME(x); }
+#endif
+AETHER_MATH_PRED(isnan)
+AETHER_MATH_PRED(isinf)
+#undef AETHER_MATH_PRED
 
 /** -1, 0 or +1 (the sign of math/round.h's sign(), NaN -> 0). */
 template <class T>
