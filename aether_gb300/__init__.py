@@ -16,9 +16,10 @@ import threading
 from . import _abi
 from ._abi import AetherError, lowering
 from .expr import (Expr, Generator, IrContext, Operand, Scalar, clamp, constant, cwiseAbs, cwiseAcos, cwiseAsin,
-                   cwiseAtan, cwiseCos, cwiseDiv, cwiseExp, cwiseExpm1, cwiseLog, cwiseLog1p, cwiseMax, cwiseMin,
-                   cwisePow, cwiseRsqrt, cwiseSign, cwiseSin, cwiseSqrt, cwiseSquare, cwiseTan, cwiseTanh, literal,
-                   plan_text, select, splitmix64, stack)
+                   cwiseAtan, cwiseCbrt, cwiseCeil, cwiseCos, cwiseCosh, cwiseDiv, cwiseErf, cwiseExp, cwiseExp2,
+                   cwiseExpm1, cwiseFloor, cwiseLog, cwiseLog10, cwiseLog1p, cwiseLog2, cwiseMax, cwiseMin, cwiseMul,
+                   cwisePow, cwiseRsqrt, cwiseSign, cwiseSin, cwiseSinh, cwiseSqrt, cwiseSquare, cwiseTan, cwiseTanh,
+                   cwiseTrunc, literal, plan_text, select, splitmix64, stack)
 
 CAPACITY_ALIGNMENT = 32
 _DTYPES = {"f64": 8, "f32": 4}
@@ -441,7 +442,9 @@ __all__ = [
     "pinned_empty",
     "Array", "Plan", "Launch", "AetherError", "Generator", "Expr", "assign", "assign_add", "assign_sub", "global_sum",
     "prepare", "get_plan", "quantized_capacity", "constant", "literal", "stack", "select", "clamp", "cwiseAbs",
-    "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCos", "cwiseDiv", "cwiseExp", "cwiseExpm1", "cwiseLog", "cwiseLog1p",
+    "cwiseAcos", "cwiseAsin", "cwiseAtan", "cwiseCbrt", "cwiseCeil", "cwiseCos", "cwiseCosh", "cwiseDiv", "cwiseErf",
+    "cwiseExp", "cwiseExp2", "cwiseExpm1", "cwiseFloor", "cwiseLog", "cwiseLog10", "cwiseLog1p", "cwiseLog2",
+    "cwiseMul", "cwiseSinh", "cwiseTrunc",
     "cwiseMax", "cwiseMin", "cwisePow", "cwiseRsqrt", "cwiseSign", "cwiseSin", "cwiseSqrt", "cwiseSquare", "cwiseTan",
     "cwiseTanh", "splitmix64", "lowering",
 ]

@@ -310,6 +310,21 @@ cwiseTanh = _unary("tanh")
 cwiseAbs = _unary("abs")
 cwiseSign = _unary("sign")
 cwiseSquare = _unary("sq")
+cwiseSinh = _unary("sinh")
+cwiseCosh = _unary("cosh")
+cwiseExp2 = _unary("exp2")
+cwiseLog2 = _unary("log2")
+cwiseLog10 = _unary("log10")
+cwiseCbrt = _unary("cbrt")
+cwiseErf = _unary("erf")
+cwiseFloor = _unary("floor")
+cwiseCeil = _unary("ceil")
+cwiseTrunc = _unary("trunc")
+
+
+def cwiseMul(l, r):
+    """Hadamard product (expr/nodes/Elementwise.h cwiseMul): the same node as l * r."""
+    return l * r
 
 
 def cwiseMin(e, o):

@@ -541,3 +541,30 @@ def test_launch_errors_are_reported():
         ag.prepare(s, x.view().dot(x.view()), op="setsum")(None)
     with pytest.raises(ag.AetherError, match="rank-0"):
         ag.prepare(a, a.view(), op="setsum")
+
+
+EXTRA_NODES = {"cwiseSinh": ("sinh", 3), "cwiseCosh": ("cosh", 3), "cwiseExp2": ("exp2", 2), "cwiseLog2": ("log2", 2),
+               "cwiseLog10": ("log10", 2), "cwiseCbrt": ("cbrt", 4), "cwiseErf": ("erf", 3), "cwiseFloor": ("floor", 0),
+               "cwiseCeil": ("ceil", 0), "cwiseTrunc": ("trunc", 0)}
+
+
+@pytest.mark.parametrize("math", [0, 1, 3])
+@pytest.mark.parametrize("fn", sorted(EXTRA_NODES))
+def test_extra_elementwise_nodes(oracle, fn, math):
+    """The rest of the elementwise node set, in every f64 lowering (the
+    emulated and FP64-grade ones reach CUDA's functions per lane for these),
+    against the oracle: rounding nodes bit for bit, the others within the
+    device-versus-host ulp table."""
+    op, ulps = EXTRA_NODES[fn]
+    n = 4099
+    x = ag.Array("f64", (3,), n)
+    ag.assign(x, ag.Generator(61).uniform(3, -6.0, 6.0))
+    arg = ag.cwiseAbs(x.view()) if op in ("log2", "log10") else x.view()
+    e = getattr(ag, fn)(arg)
+    d = ag.Array("f64", (3,), n)
+    ag.assign(d, e, math=math, contract=0)
+    ref, _ = _oracle_eval(oracle, e, "f64", (3,), n)
+    if ulps == 0:
+        assert np.array_equal(d.host(), ref[:, :n]), fn
+    else:
+        assert_ulp(d.host(), ref[:, :n], ulps, None, "%s, math %d" % (fn, math))
