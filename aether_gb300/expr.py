@@ -118,6 +118,25 @@ class Expr:
     def sum(self):
         return Node("sum", (self,), ())
 
+    def rSquaredNorm(self):
+        """1 / |e|^2 (Expression.h:182)."""
+        return Node("div", (Literal(1.0), self.squaredNorm()), ())
+
+    def cubedNorm(self):
+        """|e|^2 |e| (Expression.h:183)."""
+        return Node("mul", (self.squaredNorm(), self.norm()), ())
+
+    def rCubedNorm(self):
+        """1 / (|e|^2 |e|) (Expression.h:184)."""
+        return Node("div", (Literal(1.0), self.cubedNorm()), ())
+
+    def matDot(self, o):
+        """Sum over every component of e * o, matrices included (Expression.h:205-207)."""
+        n = 1
+        for d in self.shape:
+            n *= d
+        return self.reshape((n,)).dot(o.reshape((n,)))
+
     def maxNorm(self):
         return Node("maxnorm", (self,), ())
 
@@ -138,6 +157,14 @@ class Expr:
 
     def asPureQuaternion(self):
         return Node("pureq", (self,), (4,))
+
+    def quatReciprocal(self):
+        """conj(q) / |q|^2 (Expression.h:220-222)."""
+        return Node("scale", (self.quatConj(), self.rSquaredNorm()), (4,))
+
+    def asBack3DVector(self):
+        """The vector part (x, y, z) of a quaternion (Expression.h:228)."""
+        return self.tail(3)
 
     def inverse(self):
         return Node("inv", (self,), self.shape)
