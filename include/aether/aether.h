@@ -43,6 +43,7 @@
 #include "aether/launch.h"
 #include "aether/partition.h"
 #include "aether/runtime.h"
+#include "aether/dlpack.h"
 
 namespace aether {
 inline constexpr int version_major = 0;
