@@ -16,9 +16,9 @@
 // 64/32/16/8 bits and bool pass, one lane), a device other than the host,
 // CUDA or page-locked host memory, a negative extent or stride, a span past
 // int64 -- throw aether::Error after calling the deleter once: the import
-// owned the tensor from the moment it was handed over. RuntimeView carries
-// no device, so the import returns it beside the view and the export takes
-// it as an argument.
+// owned the tensor from the moment it was handed over. The imported view
+// carries the producer's device; RuntimeView::as<StaticViewT>() promotes it
+// to a typed view.
 //
 // The DLPack structures are the published ABI of the DLPack project (v1.0),
 // declared here field for field so that producers and consumers built
@@ -151,10 +151,10 @@ private:
     DLManagedTensorVersioned* versioned_ = nullptr;
 };
 
-/** An imported tensor: its descriptor, its device and the owner of its memory. */
+/** An imported tensor: its descriptor (with its device) and the owner of its
+ *  memory. */
 struct DLPackImport {
     RuntimeView view{};
-    Device device{};
     DLPackOwner owner;
 };
 
@@ -208,6 +208,7 @@ inline RuntimeView viewOf(const DLTensor& t) {
     r.dtype_bits = t.dtype.bits;
     r.dtype_lanes = t.dtype.lanes;
     r.rank = t.ndim;
+    r.device = Device(int(t.device.device_type), t.device.device_id);
     const unsigned __int128 lim = uint64_t(INT64_MAX);
     unsigned __int128 step = 1, span = 1;
     bool empty = false;
@@ -238,7 +239,6 @@ DLPackImport import_(M* managed, DLPackOwner owner, const char* type) {
     DLPackImport im;
     im.owner = std::move(owner);   // owns the tensor from here: a refusal below still deletes it once
     im.view = viewOf(managed->dl_tensor);
-    im.device = Device(int(managed->dl_tensor.device.device_type), managed->dl_tensor.device.device_id);
     return im;
 }
 
@@ -275,22 +275,22 @@ inline DLPackImport fromDLPack(DLManagedTensorVersioned* managed) {
 
 namespace detail {
 /** The checks both exports share (interop/DLPack.h:383-396); the dtype to write. */
-inline DLDataType exportable(const char* op, const RuntimeView& view, Device dev) {
+inline DLDataType exportable(const char* op, const RuntimeView& view) {
     if (view.rank < 0 || view.rank > AETHER_RT_RANK_CAP)
         refuse(op, "rank " + std::to_string(view.rank) + " exceeds RuntimeView's cap");
     const DLDataType dt{view.dtype_code, view.dtype_bits, view.dtype_lanes};
     if (!dtypeIsSupported(dt)) refuse(op, "unsupported dtype");
-    if (!deviceIsKnown(dev.type)) refuse(op, "unknown/unsupported device kind");
+    if (!deviceIsKnown(view.device.type)) refuse(op, "unknown/unsupported device kind");
     return dt;
 }
 template <class M>
-M* exportInto(M* t, const RuntimeView& view, Device dev, DLDataType dt) {
+M* exportInto(M* t, const RuntimeView& view, DLDataType dt) {
     auto* ctx = new ExportCtx();
     ctx->shape.assign(view.extents, view.extents + view.rank);
     ctx->strides.assign(view.strides, view.strides + view.rank);
     t->manager_ctx = ctx;
     t->dl_tensor.data = view.data;
-    t->dl_tensor.device = DLDevice{DLDeviceType(dev.type), int32_t(dev.id)};
+    t->dl_tensor.device = DLDevice{DLDeviceType(view.device.type), int32_t(view.device.id)};
     t->dl_tensor.ndim = view.rank;
     t->dl_tensor.dtype = dt;
     t->dl_tensor.shape = ctx->shape.data();
@@ -304,36 +304,36 @@ inline void deleteExportedLegacy(DLManagedTensor* self) {
 }
 }  // namespace detail
 
-/** Export a descriptor of memory on `dev` as a DLPack 1.0 tensor; the
+/** Export a descriptor as a DLPack 1.0 tensor on the view's device; the
  *  receiver calls its deleter, which frees the export's own allocations, not
  *  the data (interop/DLPack.h:383-420). */
-inline DLManagedTensorVersioned* toDLPack(const RuntimeView& view, Device dev) {
-    const DLDataType dt = detail::exportable("aether::interop::toDLPack", view, dev);
+inline DLManagedTensorVersioned* toDLPack(const RuntimeView& view) {
+    const DLDataType dt = detail::exportable("aether::interop::toDLPack", view);
     auto* t = new DLManagedTensorVersioned{};
     t->version = DLPackVersion{DLPACK_MAJOR_VERSION, DLPACK_MINOR_VERSION};
     t->deleter = &detail::deleteExported;
     t->flags = 0;
-    return detail::exportInto(t, view, dev, dt);
+    return detail::exportInto(t, view, dt);
 }
-/** A typed view, through fromView and the view's own device. */
+/** A typed view, through fromView. */
 template <class T, class X, class L, bool Vo, bool RO>
 DLManagedTensorVersioned* toDLPack(const View<T, X, L, Vo, RO>& v) {
-    return toDLPack(fromView(v), v.device());
+    return toDLPack(fromView(v));
 }
 
 /** Export as a pre-1.0 DLManagedTensor (interop/DLPackLegacy.h). The legacy
  *  type-code enum has no bool, so a bool view leaves as 8-bit unsigned, the
  *  nearest code a legacy consumer reads. */
-inline DLManagedTensor* toDLPackLegacy(const RuntimeView& view, Device dev) {
-    DLDataType dt = detail::exportable("aether::interop::toDLPackLegacy", view, dev);
+inline DLManagedTensor* toDLPackLegacy(const RuntimeView& view) {
+    DLDataType dt = detail::exportable("aether::interop::toDLPackLegacy", view);
     if (dt.code == kDLBool) dt.code = kDLUInt;
     auto* t = new DLManagedTensor{};
     t->deleter = &detail::deleteExportedLegacy;
-    return detail::exportInto(t, view, dev, dt);
+    return detail::exportInto(t, view, dt);
 }
 template <class T, class X, class L, bool Vo, bool RO>
 DLManagedTensor* toDLPackLegacy(const View<T, X, L, Vo, RO>& v) {
-    return toDLPackLegacy(fromView(v), v.device());
+    return toDLPackLegacy(fromView(v));
 }
 
 }  // namespace interop

@@ -59,7 +59,7 @@ void importLegacy() {
         CHECK(imp.view.rank == 2 && imp.view.extents[0] == 3 && imp.view.extents[1] == 8);
         CHECK(imp.view.strides[0] == 8 && imp.view.strides[1] == 1);
         CHECK(imp.view.dtype_code == kDLFloat && imp.view.dtype_bits == 64 && imp.view.dtype_lanes == 1);
-        CHECK(imp.device == aether::Device(aether::kDLCPU));
+        CHECK(imp.view.device == aether::Device(aether::kDLCPU));
         CHECK(imp.owner.owns());
         CHECK(g_legacy == 0);
         aether::interop::DLPackOwner moved = std::move(imp.owner);   // the owner moves, the deleter does not run
@@ -84,8 +84,8 @@ void importVersioned() {
         // null strides: compact row-major
         CHECK(imp.view.strides[0] == 5 && imp.view.strides[1] == 1);
         CHECK(imp.view.dtype_bits == 32);
-        CHECK(imp.device == aether::Device(aether::kDLCUDA, 3));
-        CHECK(!aether::interop::hostAccessible(imp.device.type));
+        CHECK(imp.view.device == aether::Device(aether::kDLCUDA, 3));
+        CHECK(!aether::interop::hostAccessible(imp.view.device.type));
     }
     CHECK(g_versioned == 1);
 }
@@ -211,7 +211,8 @@ void roundTrips() {
     v.strides[0] = 16;   // plane pitch larger than the sample count
     v.strides[1] = 1;
     for (const aether::Device dev : {aether::Device(aether::kDLCPU), aether::Device(aether::kDLCUDA, 1)}) {
-        DLManagedTensorVersioned* ex = aether::interop::toDLPack(v, dev);
+        v.device = dev;
+        DLManagedTensorVersioned* ex = aether::interop::toDLPack(v);
         CHECK(ex->version.major == DLPACK_MAJOR_VERSION && ex->version.minor == DLPACK_MINOR_VERSION);
         CHECK(ex->flags == 0 && ex->dl_tensor.byte_offset == 0);
         CHECK(ex->dl_tensor.device.device_type == DLDeviceType(dev.type) && ex->dl_tensor.device.device_id == dev.id);
@@ -219,7 +220,7 @@ void roundTrips() {
         CHECK(back.view.data == v.data && back.view.rank == 2);
         CHECK(std::memcmp(back.view.extents, v.extents, sizeof v.extents) == 0);
         CHECK(std::memcmp(back.view.strides, v.strides, sizeof v.strides) == 0);
-        CHECK(back.device == dev);
+        CHECK(back.view.device == dev);
     }
     // every supported dtype survives both directions, both generations
     const DLDataType kinds[] = {{kDLFloat, 64, 1}, {kDLFloat, 32, 1}, {kDLFloat, 16, 1}, {kDLBfloat, 16, 1},
@@ -229,13 +230,14 @@ void roundTrips() {
     for (const DLDataType dt : kinds) {
         v.dtype_code = dt.code;
         v.dtype_bits = dt.bits;
-        DLManagedTensorVersioned* ex = aether::interop::toDLPack(v, aether::Device(aether::kDLCPU));
+        v.device = aether::Device(aether::kDLCPU);
+        DLManagedTensorVersioned* ex = aether::interop::toDLPack(v);
         CHECK(ex->dl_tensor.dtype.code == dt.code && ex->dl_tensor.dtype.bits == dt.bits);
         {
             auto back = aether::interop::fromDLPack(ex);
             CHECK(back.view.dtype_code == dt.code && back.view.dtype_bits == dt.bits);
         }
-        DLManagedTensor* lg = aether::interop::toDLPackLegacy(v, aether::Device(aether::kDLCPU));
+        DLManagedTensor* lg = aether::interop::toDLPackLegacy(v);
         // the legacy code table has no bool: it leaves as 8-bit unsigned
         CHECK(lg->dl_tensor.dtype.code == (dt.code == kDLBool ? uint8_t(kDLUInt) : dt.code));
         CHECK(lg->dl_tensor.dtype.bits == dt.bits);
@@ -246,7 +248,7 @@ void roundTrips() {
     v.dtype_code = kDLComplex;
     bool threw = false;
     try {
-        aether::interop::toDLPack(v, aether::Device(aether::kDLCPU));
+        aether::interop::toDLPack(v);
     } catch (const aether::Error& e) {
         threw = std::string(e.what()).find("aether::interop::toDLPack failed") != std::string::npos;
     }
@@ -255,7 +257,8 @@ void roundTrips() {
     v.dtype_bits = 64;
     threw = false;
     try {
-        aether::interop::toDLPackLegacy(v, aether::Device(4));
+        v.device = aether::Device(4);
+        aether::interop::toDLPackLegacy(v);
     } catch (const aether::Error& e) {
         threw = std::string(e.what()).find("unknown/unsupported device kind") != std::string::npos;
     }
@@ -269,6 +272,66 @@ void roundTrips() {
     ex->deleter(ex);
 }
 
+template <class V>
+bool promotionRefused(const aether::RuntimeView& r, const char* needle) {
+    try {
+        (void)r.as<V>();
+    } catch (const aether::Error& e) {
+        const std::string w = e.what();
+        if (w.find("aether::RuntimeView::as failed") != std::string::npos && w.find(needle) != std::string::npos)
+            return true;
+        std::printf("unexpected message: %s\n", w.c_str());
+    }
+    return false;
+}
+
+// RuntimeView::as<StaticViewT>(): a DLPack import promoted back onto typed
+// views (tests/test_DLPackRoundtrip.cu:278-298), and its refusals
+void promotions() {
+    const std::size_t n = 5;
+    std::vector<double> soa(3 * n);
+    for (std::size_t i = 0; i < soa.size(); ++i) soa[i] = double(i);
+    auto tv = aether::make_view<double, 3, aether::dyn>(soa.data(), aether::Device(aether::kDLCUDA), n);
+    auto back = aether::interop::fromDLPack(aether::interop::toDLPack(tv));
+    const aether::Vec3dView promoted = back.view.as<aether::Vec3dView>();
+    CHECK(promoted.data() == tv.data() && promoted.device() == aether::Device(aether::kDLCUDA));
+    CHECK(promoted.extent(1) == n && promoted.mapping().stride(0) == n);
+    CHECK(back.view.size() == int64_t(3 * n));
+
+    // a padded plane layout promotes onto a layout_stride view only
+    aether::RuntimeView r{};
+    r.data = soa.data();
+    r.dtype_code = 2;
+    r.dtype_bits = 64;
+    r.dtype_lanes = 1;
+    r.rank = 2;
+    r.extents[0] = 2;
+    r.extents[1] = 4;
+    r.strides[0] = 6;
+    r.strides[1] = 1;
+    r.device = aether::Device(aether::kDLCPU);
+    using Strided = aether::View<double, aether::extents<2, aether::dyn>, aether::layout_stride>;
+    const Strided sv = r.as<Strided>();
+    CHECK(sv(1, 3) == soa[9] && sv(0, 2) == soa[2]);
+    using V2d = aether::VecView<double, 2>;
+    using V2f = aether::VecView<float, 2>;
+    CHECK(promotionRefused<V2d>(r, "not row-major"));
+    CHECK(promotionRefused<aether::Vec3dView>(r, "extent 0 is 2, the view's is 3"));
+    CHECK(promotionRefused<V2f>(r, "dtype mismatch"));
+    CHECK(promotionRefused<aether::ScalarView<double>>(r, "rank 2 != the view's 1"));
+    r.device = aether::Device(4);
+    CHECK(promotionRefused<Strided>(r, "unknown/unsupported device kind (type=4)"));
+    r.device = aether::Device(aether::kDLCPU);
+    r.strides[0] = int64_t(1) << 33;
+    CHECK(promotionRefused<Strided>(r, "32-bit offsets"));
+    // a const view of floats, rank 1
+    std::vector<float> f(7, 1.5f);
+    auto fv = aether::make_view<const float, aether::dyn>(f.data(), aether::Device(aether::kDLCPU), f.size());
+    const aether::RuntimeView fr = aether::fromView(fv);
+    CHECK(fr.dtype_bits == 32 && fr.size() == 7);
+    CHECK(fr.as<aether::ScalarView<const float>>()(6) == 1.5f);
+}
+
 }  // namespace
 
 int main() {
@@ -277,6 +340,7 @@ int main() {
     importBoolAndRawBits();
     rejections();
     roundTrips();
+    promotions();
     if (failures) return 1;
     std::printf("dlpack ok\n");
     return 0;
