@@ -12,9 +12,8 @@
 // The array is a file-scope static __device__ buffer of AG_NOALLOC_SCRATCH_BYTES
 // (1 MiB) that every GPU which loads the library holds until the process
 // exits. Its device address is resolved once per device, on the first call
-// made with that device current (cudaGetSymbolAddress), so that first call
-// should come before any stream capture; a first call on a capturing stream
-// is refused. The address is kept for the life of the process: after a
+// made with that device current (cudaGetSymbolAddress); a first call on a
+// stream that is capturing is refused. The address is kept for the life of the process: after a
 // cudaDeviceReset the entry point is not usable, as plans are not. All calls
 // share the one array: the counter is cleared at the start of every call, and
 // calls whose kernels overlap on the GPU (two streams, or two threads) race

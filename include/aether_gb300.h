@@ -198,10 +198,10 @@ int aether_plan_launch_many(void* const* plans, const AetherLaunch* args, int co
  * chunk, 16 + 16 * chunks bytes) comes from a 1 MiB array compiled into the
  * library that every GPU which loads it holds until exit; sizes that need more
  * are refused with an error naming the limit. `args->workspace` must be NULL.
- * The first call on a device resolves the array's address and should come
- * before any stream capture (a first call on a capturing stream is refused);
- * the address is kept for the process, so the entry point is not usable after
- * a cudaDeviceReset. Calls share the array (the counter is cleared at each
+ * The first call on a device resolves the array's address (a first call on a
+ * stream that is capturing is refused with an error saying so); the address
+ * is kept for the process, so the entry point is not usable after a
+ * cudaDeviceReset. Calls share the array (the counter is cleared at each
  * call), so calls whose kernels overlap on the GPU race and must be
  * serialised by the caller. */
 int aether_plan_launch_noalloc(void* plan, const AetherLaunch* args, void* stream);
