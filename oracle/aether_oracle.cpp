@@ -919,6 +919,34 @@ double orc_normal_f64(uint64_t seed, uint32_t global, uint64_t counter) {
     return normal_d<double>(seed, global, counter);
 }
 float orc_normal_f32(uint64_t seed, uint32_t global, uint64_t counter) { return normal_f(seed, global, counter); }
+// The keyed block of (seed, global, counter) and the word -> real conversions
+// themselves (Backend.h:75-101, :123-131, :152-157).
+void orc_philox_block(uint64_t seed, uint32_t global, uint64_t counter, uint32_t out[4]) {
+    const Q4 r = block(seed, global, counter);
+    out[0] = r.x;
+    out[1] = r.y;
+    out[2] = r.z;
+    out[3] = r.w;
+}
+double orc_u01_from_word_f64(uint32_t w) { return u01d(w); }
+float orc_u01_from_word_f32(uint32_t w) { return u01f(w); }
+double orc_u01_hq(uint32_t x, uint32_t y) { return u01hq(x, y); }
+// Mean and standard error of z^2 z'^2 over n seeds splitmix64(salt + k), z at
+// counter 5 and z' at counter 5 + lag of global 0: 1 for independent standard
+// normals (tests/test_RandomIndependence.cpp:29-48).
+void orc_lag_fourth_moment(uint64_t salt, uint64_t lag, int n, int f32, double* mean, double* se) {
+    double sum = 0.0, sum2 = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const uint64_t seed = splitmix(salt + uint64_t(k));
+        const double z = f32 ? double(normal_f(seed, 0, 5)) : normal_d<double>(seed, 0, 5);
+        const double y = f32 ? double(normal_f(seed, 0, 5 + lag)) : normal_d<double>(seed, 0, 5 + lag);
+        const double q = z * z * y * y;
+        sum += q;
+        sum2 += q * q;
+    }
+    *mean = sum / n;
+    *se = std::sqrt((sum2 / n - *mean * *mean) / n);
+}
 
 const char* orc_last_error(void) { return g_err.c_str(); }
 

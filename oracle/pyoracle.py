@@ -67,6 +67,11 @@ def lib():
             "orc_cfg1_f64": (None, [P, P, P, P, u64, u64, i]),
             "orc_cfg2a_f64": (None, [P, P, P, P, P, u64, u64, i]),
             "orc_max_threads": (i, []),
+            "orc_philox_block": (None, [u64, u32, u64, P]),
+            "orc_u01_from_word_f64": (d, [u32]),
+            "orc_u01_from_word_f32": (f, [u32]),
+            "orc_u01_hq": (d, [u32, u32]),
+            "orc_lag_fourth_moment": (None, [u64, u64, i, i, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -78,6 +83,20 @@ def lib():
 
 def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def philox_block(seed, global_, counter):
+    """The four words of the keyed Philox block of (seed, global, counter)."""
+    out = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox_block(seed, global_, counter, _ptr(out))
+    return out
+
+
+def lag_fourth_moment(salt, lag, n, f32=False):
+    """(mean, standard error) of z^2 z'^2 over n seeds, z' `lag` counters on."""
+    m, se = ctypes.c_double(), ctypes.c_double()
+    lib().orc_lag_fourth_moment(salt, lag, n, int(f32), ctypes.byref(m), ctypes.byref(se))
+    return m.value, se.value
 
 
 def generator_key(seed, stream_id=0):
