@@ -90,3 +90,56 @@ def test_atomic_accumulation_from_two_streams():
     exact = np.array([[math.fsum(terms[:, c, i]) for i in range(n)] for c in range(3)])
     err = np.abs(got - exact) / np.spacing(np.abs(exact))
     assert err.max() <= 2.0, err.max()
+
+
+def _profiles(bodies, n, seed):
+    """Two families of per-body terms (bodies x 3 x n): a magnitude spread
+    over eleven decades with mixed signs, and a cancellation family of
+    +-A (1 - d) pairs whose differences d run from 0 to 1e-3."""
+    rng = np.random.default_rng(seed)
+    jit = 1.0 + 0.4375 * rng.random((bodies, 3, n))
+    rel = np.array([1.0, 1.1e-3, 3.1e-6, 6.0e-7, 5.0e-8, 1.0e-10, 4.0e-12, 8.0e-13])
+    sign = rng.choice([-1.0, 1.0], size=(bodies, 3, n))
+    sign[0] = 1.0
+    spread = 8.0e-3 * rel[np.arange(bodies) % 8][:, None, None] * jit * sign
+    dl = np.array([0.0, 2.22e-16, 9.1e-13, 9.3e-10, 9.5e-7, 9.8e-4])[np.arange(n) % 6]
+    A = 1.0e-2 * jit
+    cancel = np.where((np.arange(bodies) % 2 == 0)[:, None, None], A, -A * (1.0 - dl))
+    return {"spread": spread, "cancel": cancel}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("profile", ["spread", "cancel"])
+def test_atomic_accumulation_bitwise_under_permuted_launch_orders(profile):
+    """One launch per body in four orders (identity, reverse, two shuffles),
+    alternating two streams: every order delivers the same bits
+    (tests/test_AccumOrderPermutation.cu), within an ulp of the exact sum."""
+    _gpu()
+    bodies, n = 8, 128
+    terms = _profiles(bodies, n, 11)[profile]
+    arrs = []
+    for k in range(bodies):
+        a = ag.Array("f64", (3,), n)
+        a.upload(terms[k])
+        arrs.append(a)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(3)
+    orders = [list(range(bodies)), list(reversed(range(bodies))), list(rng.permutation(bodies)),
+              list(rng.permutation(bodies))]
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    delivered = []
+    for order in orders:
+        plane = ag.AccumPlane((3,), n)
+        torch.cuda.synchronize()
+        for j, k in enumerate(order):
+            plane.add(arrs[k].view() * 1.0, atomic=True, stream=(s1 if j % 2 else s2).cuda_stream)
+        s1.synchronize()
+        s2.synchronize()
+        delivered.append(plane.delivered().host().copy())
+    for d in delivered[1:]:
+        assert np.array_equal(d.view(np.int64), delivered[0].view(np.int64))
+    exact = np.array([[math.fsum(terms[:, c, i]) for i in range(n)] for c in range(3)])
+    nz = exact != 0.0
+    err = np.abs(delivered[0][nz] - exact[nz]) / np.spacing(np.abs(exact[nz]))
+    assert err.max() <= 1.0, err.max()
+    assert np.all(delivered[0][~nz] == 0.0)
