@@ -254,4 +254,40 @@ AETHER_DEVICEANDHOST() constexpr auto evalW(const E& e, const SampleIndex& i) {
     return e.template eval<Is...>(i);
 }
 
+// The reduction operators by their public names, called as
+// `SumOp<T>{}(a, b)` (expr/Reduce.h:53-86).
+template <class T>
+struct SumOp {
+    AETHER_DEVICEANDHOST() constexpr T operator()(T a, T b) const { return a + b; }
+};
+template <class T>
+struct TimesOp {
+    AETHER_DEVICEANDHOST() constexpr T operator()(T a, T b) const { return a * b; }
+};
+template <class T>
+struct MaxOp {
+    AETHER_DEVICEANDHOST() constexpr T operator()(T a, T b) const { return a > b ? a : b; }
+};
+struct LogicalAndOp {
+    AETHER_DEVICEANDHOST() constexpr bool operator()(bool a, bool b) const { return a && b; }
+};
+
+namespace detail {
+template <class E, std::size_t... K>
+AETHER_DEVICEANDHOST() bool all_finite_(const E& e, const SampleIndex& i, std::index_sequence<K...>) {
+    bool ok = true;
+    ((ok = LogicalAndOp{}(math::isfinite(e.template eval<K>(i)), ok)), ...);
+    return ok;
+}
+}  // namespace detail
+
+/** True when every component of a rank-1 expression is finite, at sample 0
+ *  like the member reductions (expr/Reduce.h:198-211). */
+template <class E, class = std::enable_if_t<aether_expression<E>>>
+AETHER_DEVICEANDHOST() bool isFinite(const E& e) {
+    static_assert(detail::extents_of<E>::Rank == 1, "isFinite: only rank-1 expressions are supported");
+    return detail::all_finite_(e, SampleIndex::make(std::size_t(0)),
+                               std::make_index_sequence<detail::extents_of<E>::static_extent(0)>{});
+}
+
 }  // namespace aether

@@ -58,6 +58,16 @@ public:
         for (std::size_t k = 0; k < Size; ++k) m.data_[k] = (k % (n + 1) == 0) ? T(1) : T(0);
         return m;
     }
+    // The reference's factory spellings (view/Item.h:195-225).
+    AETHER_DEVICEANDHOST() static constexpr Item Identity() { return identity(); }
+    AETHER_DEVICEANDHOST() static constexpr Item filled(const T& v) {
+        Item m{};
+        for (std::size_t k = 0; k < Size; ++k) m.data_[k] = v;
+        return m;
+    }
+    AETHER_DEVICEANDHOST() static constexpr Item Zeros() { return filled(T(0)); }
+    AETHER_DEVICEANDHOST() static constexpr Item Ones() { return filled(T(1)); }
+    AETHER_DEVICEANDHOST() static constexpr std::size_t size() { return Size; }
 
     template <class... I>
     AETHER_DEVICEANDHOST() constexpr T& operator()(I... idx) {
