@@ -44,6 +44,7 @@
 #include "aether/partition.h"
 #include "aether/runtime.h"
 #include "aether/dlpack.h"
+#include "aether/buffer.h"
 
 namespace aether {
 inline constexpr int version_major = 0;

@@ -29,6 +29,7 @@
 #include <climits>
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <string>
 #include <utility>
 #include <vector>
@@ -40,6 +41,8 @@
 #define DLPACK_DLPACK_H_
 #define DLPACK_MAJOR_VERSION 1
 #define DLPACK_MINOR_VERSION 0
+#define DLPACK_FLAG_BITMASK_READ_ONLY (1UL << 0UL)
+#define DLPACK_FLAG_BITMASK_IS_COPIED (1UL << 1UL)
 extern "C" {
 typedef struct {
     uint32_t major;
@@ -177,6 +180,15 @@ inline bool deviceIsKnown(int type) {
     return type == ::kDLCPU || type == ::kDLCUDA || type == ::kDLCUDAHost;
 }
 
+// The device code as the producer wrote it: read as the int32 it is on the
+// wire, since a code outside the enumerators is no valid DLDeviceType value.
+inline int rawDeviceType(const DLDevice& d) {
+    static_assert(sizeof(d.device_type) == sizeof(int32_t), "DLDeviceType is an int32 on the wire");
+    int32_t v;
+    std::memcpy(&v, &d.device_type, sizeof v);
+    return v;
+}
+
 [[noreturn]] inline void refuse(const std::string& op, const std::string& why) {
     throw Error::memory(op, "DLPack", 0, why);
 }
@@ -195,8 +207,8 @@ inline RuntimeView viewOf(const DLTensor& t) {
         refuse(op, "unsupported dtype (code=" + std::to_string(unsigned(t.dtype.code)) +
                        ", bits=" + std::to_string(unsigned(t.dtype.bits)) +
                        ", lanes=" + std::to_string(unsigned(t.dtype.lanes)) + ")");
-    if (!deviceIsKnown(int(t.device.device_type)))
-        refuse(op, "unknown/unsupported device kind (type=" + std::to_string(int(t.device.device_type)) + ")");
+    const int kind = rawDeviceType(t.device);
+    if (!deviceIsKnown(kind)) refuse(op, "unknown/unsupported device kind (type=" + std::to_string(kind) + ")");
     for (int k = 0; k < t.ndim; ++k) {
         if (t.shape[k] < 0) refuse(op, "shape[" + std::to_string(k) + "]=" + std::to_string(t.shape[k]) + " is negative");
         if (t.strides && t.strides[k] < 0)
@@ -208,7 +220,7 @@ inline RuntimeView viewOf(const DLTensor& t) {
     r.dtype_bits = t.dtype.bits;
     r.dtype_lanes = t.dtype.lanes;
     r.rank = t.ndim;
-    r.device = Device(int(t.device.device_type), t.device.device_id);
+    r.device = Device(kind, t.device.device_id);
     const unsigned __int128 lim = uint64_t(INT64_MAX);
     unsigned __int128 step = 1, span = 1;
     bool empty = false;

@@ -1,9 +1,12 @@
 """aether::interop's C++ DLPack import and export (include/aether/dlpack.h;
-interop/DLPack.h:226-430 and interop/DLPackLegacy.h).
+interop/DLPack.h:226-430 and interop/DLPackLegacy.h) and its buffer layer
+(include/aether/buffer.h; interop/Buffer.h).
 
 CPU: tests/cpp/dlpack_interop.cpp, the reference's import, refusal and
-round-trip cases (tests/test_DLPackRoundtrip.cu, tests/test_DLPackDtypes_common.h)
-over producers whose deleters count their calls, run under the address and
+round-trip cases (tests/test_DLPackRoundtrip.cu, tests/test_DLPackDtypes_common.h),
+and tests/cpp/buffer_interop.cpp, the buffer layer's (aether/buffer.h,
+tests/test_DLPackBuffer_common.h), over producers whose deleters count their
+calls, run under the address and
 undefined-behaviour sanitizers; the same source against the DLPack project's
 own header as torch ships it, whose struct layout must equal ours byte for
 byte; the header in a CUDA translation unit.
@@ -22,6 +25,7 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.join(REPO, "aether_gb300", "lib")
 SRC = os.path.join(REPO, "tests", "cpp", "dlpack_interop.cpp")
+BUFFER_SRC = os.path.join(REPO, "tests", "cpp", "buffer_interop.cpp")
 
 
 def _cxx():
@@ -39,25 +43,41 @@ def _torch_include():
     return inc
 
 
-def _build_and_run(tmp_path, name, extra):
+def _build_and_run(tmp_path, name, extra, src=SRC, ok="dlpack ok"):
     exe = str(tmp_path / name)
-    r = subprocess.run([_cxx(), "-std=c++17", "-O1", "-g", "-Wall", "-Wextra", "-I", INCLUDE, SRC, "-o", exe] + extra,
+    r = subprocess.run([_cxx(), "-std=c++17", "-O1", "-g", "-Wall", "-Wextra", "-I", INCLUDE, src, "-o", exe] + extra,
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     run = subprocess.run([exe], capture_output=True, text=True, timeout=120)
-    assert run.returncode == 0 and "dlpack ok" in run.stdout, run.stdout + run.stderr
+    assert run.returncode == 0 and ok in run.stdout, run.stdout + run.stderr
+
+
+def _sanitizers(tmp_path):
+    probe = subprocess.run([_cxx(), "-fsanitize=address,undefined", "-x", "c++", "-", "-o", str(tmp_path / "p")],
+                           input="int main(){}", capture_output=True, text=True)
+    return ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined"] if probe.returncode == 0 else []
 
 
 def test_interop_cases_under_sanitizers(tmp_path):
-    probe = subprocess.run([_cxx(), "-fsanitize=address,undefined", "-x", "c++", "-", "-o", str(tmp_path / "p")],
-                           input="int main(){}", capture_output=True, text=True)
-    extra = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined"] if probe.returncode == 0 else []
-    _build_and_run(tmp_path, "dlpack_interop", extra)
+    _build_and_run(tmp_path, "dlpack_interop", _sanitizers(tmp_path))
 
 
 def test_interop_cases_against_the_projects_header(tmp_path):
     inc = _torch_include()
     _build_and_run(tmp_path, "dlpack_interop_torch", ["-I", inc, "-include", "ATen/dlpack.h"])
+
+
+def test_buffer_layer_under_sanitizers(tmp_path):
+    """aether/buffer.h (interop/Buffer.h): access from both DLPack generations
+    and the array interface, keep-alive chains, requirements and their
+    messages, exports that carry the read-only flag
+    (tests/test_DLPackBuffer_common.h)."""
+    _build_and_run(tmp_path, "buffer_interop", _sanitizers(tmp_path), BUFFER_SRC, "buffer ok")
+
+
+def test_buffer_layer_against_the_projects_header(tmp_path):
+    inc = _torch_include()
+    _build_and_run(tmp_path, "buffer_interop_torch", ["-I", inc, "-include", "ATen/dlpack.h"], BUFFER_SRC, "buffer ok")
 
 
 LAYOUT = r"""
