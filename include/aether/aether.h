@@ -38,6 +38,7 @@
 #include "aether/array.h"
 #include "aether/eval.h"
 #include "aether/accum.h"
+#include "aether/accum_run.h"
 #include "aether/batch.h"
 #include "aether/device_flag.h"
 #include "aether/launch.h"
