@@ -44,6 +44,9 @@
 #include "aether/launch.h"
 #include "aether/partition.h"
 #include "aether/runtime.h"
+#include "aether/reshape.h"
+#include "aether/view_copy.h"
+#include "aether/append_counter.h"
 #include "aether/dlpack.h"
 #include "aether/buffer.h"
 
