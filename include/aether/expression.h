@@ -178,7 +178,7 @@ public:
         return detail::fold_dot(derived(), derived(), SampleIndex::make(std::size_t(0)));
     }
     AETHER_DEVICEANDHOST() T norm() const { return math::sqrt(squaredNorm()); }
-    AETHER_DEVICEANDHOST() T rNorm() const { return math::rsqrt(squaredNorm()); }
+    AETHER_DEVICEANDHOST() T rNorm() const { return T(1) / math::sqrt(squaredNorm()); }   // 1 / sqrt, not rsqrt (expr/Expression.h:202-205)
     AETHER_DEVICEANDHOST() constexpr T rSquaredNorm() const { return T(1) / squaredNorm(); }
     AETHER_DEVICEANDHOST() T cubedNorm() const { return squaredNorm() * norm(); }
     AETHER_DEVICEANDHOST() T rCubedNorm() const { return T(1) / cubedNorm(); }

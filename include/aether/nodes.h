@@ -389,7 +389,7 @@ public:
         if constexpr (Kind == 0) return fold_dot(l_, r_, i);
         if constexpr (Kind == 1) return fold_dot(l_, l_, i);
         if constexpr (Kind == 2) return math::sqrt(fold_dot(l_, l_, i));
-        if constexpr (Kind == 3) return math::rsqrt(fold_dot(l_, l_, i));
+        if constexpr (Kind == 3) return element_type(1) / math::sqrt(fold_dot(l_, l_, i));
         if constexpr (Kind == 4) return fold_sum(l_, i);
         if constexpr (Kind == 5)
             return fold_maxabs_(l_, i, std::make_index_sequence<size_of<extents_of<L>>>{});
