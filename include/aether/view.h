@@ -284,4 +284,15 @@ AETHER_DEVICEANDHOST() constexpr View<T, extents<Es...>> make_view(T* ptr, D... 
     return make_view<T, Es...>(ptr, Device(kDLCUDA, 0), dynVals...);
 }
 
+/** A view of components Es... over `block_samples` block-local samples in
+ *  shared memory (view/WorkView.h): compact, components first, indexed with
+ *  SampleIndex::work(). One dynamic shared array can hold several, each
+ *  carved at its own byte offset. */
+template <class T, std::size_t... Es>
+AETHER_DEVICEANDHOST() constexpr View<T, extents<Es..., dyn>> make_work_view(T* shared_ptr, offset_t block_samples) {
+    using X = extents<Es..., dyn>;
+    return View<T, X>(shared_ptr, typename layout_right::template mapping<X>(X(std::size_t(block_samples))),
+                      Device(kDLCUDA));
+}
+
 }  // namespace aether

@@ -6,8 +6,9 @@
 // A host compiler runs the host cases: reshaping host views, and the append
 // counter's view over host words (sequential slots, 8 threads racing, the
 // overflow). nvcc -x cu, linked to the engine, adds the device cases: views
-// copied between device and page-locked host memory and the refusals, and
-// kernels appending into an Array's spare capacity up to and past it.
+// copied between device and page-locked host memory and the refusals, work
+// views staging samples in shared memory (view/WorkView.h), and kernels
+// appending into an Array's spare capacity up to and past it.
 // Prints "view tools ok".
 #include <aether/aether.h>
 
@@ -111,6 +112,28 @@ void appendViewOnHost() {
 #if defined(__CUDACC__)
 namespace {
 
+// Work views in shared memory (view/WorkView.h): a block stages its samples
+// of `a` in a static shared array and of `b` in a carve of the dynamic one,
+// then writes out[i] = a[i] + b[the mirrored sample of the same block].
+using Planes3 = aether::Array<double, 3>::ViewT;
+AETHER_KERNEL() void stageKernel(Planes3 a, Planes3 b, Planes3 out) {
+    AETHER_SHARED() double bufA[3 * 128];
+    extern __shared__ unsigned char raw[];
+    const aether::offset_t bs = blockDim.x;
+    auto wa = aether::make_work_view<double, 3>(bufA, bs);
+    auto wb = aether::make_work_view<double, 3>(reinterpret_cast<double*>(raw), bs);
+    const aether::SampleIndex i = aether::SampleIndex::make(threadIdx.x, blockIdx.x, blockDim.x);
+    const bool live = i.global() < a.samples();
+    if (live) {
+        wa[aether::SampleIndex::make(std::size_t(i.work()))] = a[i].get();
+        for (int c = 0; c < 3; ++c) wb(c, i.work()) = b(c, i.global());
+    }
+    __syncthreads();
+    const aether::offset_t mirror = bs - 1 - i.work();
+    if (live && blockIdx.x * bs + mirror < a.samples())
+        for (int c = 0; c < 3; ++c) out(c, i.global()) = wa(c, i.work()) + wb(c, mirror);
+}
+
 AETHER_KERNEL() void appendKernel(aether::accum::AppendCounterView counter,
                                   aether::View<double, aether::extents<2, aether::dyn>, aether::layout_stride> spare,
                                   unsigned n) {
@@ -156,6 +179,34 @@ void copies() {
     CHECK(thrown([&] { aether::copyAsync(shorter.deviceView(), a.deviceView(), st); }).find("extents mismatch") !=
           std::string::npos);
     AETHER_CHECK_CUDA(cudaStreamDestroy(st));
+}
+
+void workViews() {
+    const std::size_t n = 1000;   // 8 blocks of 128, the last one partial
+    aether::Array<double, 3> a(n), b(n), out(n);
+    auto ha = a.hostView();
+    auto hb = b.hostView();
+    auto ho = out.hostView();
+    for (std::size_t s = 0; s < n; ++s)
+        for (std::size_t c = 0; c < 3; ++c) {
+            ha(c, s) = double(c * 1000 + s);
+            hb(c, s) = 0.5 * double(s) - double(c);
+            ho(c, s) = -1.0;
+        }
+    a.upload();
+    b.upload();
+    out.upload();
+    stageKernel<<<(unsigned(n) + 127) / 128, 128, 3 * 128 * sizeof(double)>>>(a.deviceView(), b.deviceView(),
+                                                                               out.deviceView());
+    aether::cuda::checkLastLaunch("stageKernel");
+    out.download();
+    bool ok = true;
+    for (std::size_t s = 0; s < n; ++s) {
+        const std::size_t blk = s / 128, m = blk * 128 + (127 - s % 128);
+        for (std::size_t c = 0; c < 3; ++c)
+            ok &= out.hostView()(c, s) == (m < n ? ha(c, s) + hb(c, m) : -1.0);
+    }
+    CHECK(ok);
 }
 
 void appends() {
@@ -206,6 +257,7 @@ int main() {
     appendViewOnHost();
 #if defined(__CUDACC__)
     copies();
+    workViews();
     appends();
 #endif
     if (failures) return 1;
