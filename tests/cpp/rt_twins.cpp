@@ -5,7 +5,8 @@
 // 3x4 by 4x5; store. Items on the host, per-sample proxies view[i] over
 // arrays of samples on the host and in a kernel. Every result must equal the
 // static form's bits (built with contraction off: -ffp-contract=off on the
-// host, --fmad=false on the device). Prints "rt twins ok".
+// host, --fmad=false and -Xcompiler -ffp-contract=off in the nvcc build).
+// Prints "rt twins ok".
 #include <aether/aether.h>
 #include <aether/rt.h>
 

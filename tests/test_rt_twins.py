@@ -3,7 +3,9 @@ per-sample reductions and contractions return the bits of the static forms
 they stand in for (tests/cpp/rt_twins.cpp): dot, sum, the norm family,
 maxNorm, isFinite, matDot, matVec (=, +=, -=), matMat, transposed operands and
 store, over Items and per-sample proxies, 144-element and 8x40 operands
-included. Contraction is off in both builds, so equal means bit-equal.
+included. Contraction is off in every build (the device code and the host
+code of the nvcc build too: an aarch64 host compiler contracts by default),
+so equal means bit-equal.
 
 CPU: the host build. GPU: the same checks, one sample per thread."""
 
@@ -40,7 +42,8 @@ def _nvcc(tmp_path):
         pytest.skip("no nvcc")
     exe = str(tmp_path / "rt_twins_cu")
     r = subprocess.run([nvcc, "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-O2",
-                        "--fmad=false", "-I", INCLUDE, SRC, "-o", exe], capture_output=True, text=True)
+                        "--fmad=false", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, SRC, "-o", exe],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe
 
