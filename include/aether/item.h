@@ -124,7 +124,7 @@ private:
         assign_seq_(e, SampleIndex::make(std::size_t(0)), std::make_index_sequence<Size>{});
     }
 
-    T data_[Size ? Size : 1];
+    T data_[Size ? Size : 1]{};   // a default-constructed Item is zero (view/Item.h:275)
 };
 
 namespace detail {
@@ -170,5 +170,15 @@ template <class T, std::size_t R, std::size_t C>
 using MatView = View<T, extents<R, C, dyn>>;
 using Vec3dView = VecView<double, 3>;
 using Mat33dView = MatView<double, 3, 3>;
+
+/** K slots of D components in one Item (view/Tile.h): a plain Item<T, D*K>;
+ *  slot<s, D>(tile) is its s-th slot, a segment of the item. */
+template <class T, std::size_t D, std::size_t K>
+using Tile = Item<T, D * K>;
+template <std::size_t s, std::size_t D, class T, std::size_t N>
+AETHER_DEVICEANDHOST() constexpr auto slot(const Item<T, N>& tile) {
+    static_assert((s + 1) * D <= N, "slot<s, D>(): slot index out of range");
+    return tile.template segment<s * D, D>();
+}
 
 }  // namespace aether

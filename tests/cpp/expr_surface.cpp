@@ -1,6 +1,7 @@
 // The per-sample expression surface on Items and views, the cases of the
 // reference's tests/test_ExprDepth.cpp, test_ExprStructural, test_ExprReduce,
-// test_ItemRank0 and the Item factories of view/Item.h:195-225: a 48-operand
+// test_ItemRank0, test_Tile and the Item factories of view/Item.h:195-225
+// (a default-constructed Item is zero): a 48-operand
 // chained sum and a 24-operand sum of scaled terms, exact; head, tail and
 // segment reads alone and inside arithmetic; dot, sum, the norm family and
 // maxNorm by hand; isFinite; rank-0 items; the public reduction functors.
@@ -96,7 +97,21 @@ AETHER_DEVICEANDHOST() int items() {
     return fails;
 }
 
-AETHER_DEVICEANDHOST() int all() { return depth() + structural() + reduce() + items(); }
+AETHER_DEVICEANDHOST() int tiles() {
+    int fails = 0;
+    const aether::Tile<double, 3, 4> zero;   // a default-constructed item is zero
+    for (std::size_t k = 0; k < zero.size(); ++k) EXPECT(zero.data()[k] == 0.0);
+    const aether::Tile<double, 3, 4> t{1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0, 10.0, 11.0, 12.0};
+    const aether::Vec3d s2 = aether::slot<2, 3>(t);
+    EXPECT(s2(0) == 7.0 && s2(1) == 8.0 && s2(2) == 9.0);
+    const aether::Vec3d sum = aether::slot<0, 3>(t) + aether::slot<3, 3>(t);
+    EXPECT(sum(0) == 11.0 && sum(2) == 15.0);
+    const aether::Mat33d m;
+    EXPECT(m(1, 2) == 0.0 && m.sum() == 0.0);
+    return fails;
+}
+
+AETHER_DEVICEANDHOST() int all() { return depth() + structural() + reduce() + items() + tiles(); }
 
 #if defined(__CUDACC__)
 AETHER_KERNEL() void surface_kernel(int* fails) { *fails = all(); }
