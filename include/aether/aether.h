@@ -51,6 +51,27 @@
 #include "aether/dlpack.h"
 #include "aether/buffer.h"
 
+#include <cstdint>
+
+// Index aliases and version queries of the reference's umbrella
+// (aether/typedefs.h, aether/version.h).
+#ifndef AETHER_INDEX_T
+#define AETHER_INDEX_T std::uint32_t
+#endif
+#ifndef AETHER_VERSION_STRING
+#define AETHER_VERSION_STRING "unknown"
+#endif
+#ifndef AETHER_GIT_REVISION
+#define AETHER_GIT_REVISION "unknown"
+#endif
+
 namespace aether {
 inline constexpr int version_major = 0;
+using index_base_t = AETHER_INDEX_T;
+using idx_t = index_base_t;
+using dims_t = index_base_t;
+constexpr const char* version() { return AETHER_VERSION_STRING; }
+constexpr const char* gitRevision() { return AETHER_GIT_REVISION; }
+/** The consumer source API's tag, the reference's. */
+constexpr const char* abi() { return "aether-abi-1"; }
 }  // namespace aether

@@ -89,6 +89,7 @@ AETHER_DEVICEANDHOST() int items() {
             EXPECT(Z(r, c) == 0.0 && O(r, c) == 1.0);
         }
     EXPECT(aether::Mat33d::size() == 9);
+    EXPECT(sizeof(aether::idx_t) == 4 && sizeof(aether::dims_t) == 4 && aether::abi()[0] == 'a');
     // a rank-0 item read from a scalar view at a sample
     double plane[4] = {0.25, 0.5, 0.75, 1.0};
     const auto sv = aether::make_view<double, aether::dyn>(plane, aether::Device(aether::kDLCPU), 4);
