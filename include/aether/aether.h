@@ -70,8 +70,8 @@ inline constexpr int version_major = 0;
 using index_base_t = AETHER_INDEX_T;
 using idx_t = index_base_t;
 using dims_t = index_base_t;
-constexpr const char* version() { return AETHER_VERSION_STRING; }
-constexpr const char* gitRevision() { return AETHER_GIT_REVISION; }
+AETHER_DEVICEANDHOST() constexpr const char* version() { return AETHER_VERSION_STRING; }
+AETHER_DEVICEANDHOST() constexpr const char* gitRevision() { return AETHER_GIT_REVISION; }
 /** The consumer source API's tag, the reference's. */
-constexpr const char* abi() { return "aether-abi-1"; }
+AETHER_DEVICEANDHOST() constexpr const char* abi() { return "aether-abi-1"; }
 }  // namespace aether
