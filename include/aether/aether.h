@@ -47,6 +47,7 @@
 #include "aether/runtime.h"
 #include "aether/reshape.h"
 #include "aether/view_copy.h"
+#include "aether/chunk.h"
 #include "aether/append_counter.h"
 #include "aether/dlpack.h"
 #include "aether/buffer.h"
