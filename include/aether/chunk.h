@@ -11,7 +11,9 @@
 // page-locked memory); copyAsync() is stream-ordered and takes only pairs the
 // copy engines serve asynchronously (device and page-locked memory);
 // fill() repeats a value of 1..16 bytes over a chunk. make_view(chunk, n...)
-// views a chunk, its size checked. Errors are aether::Error in the
+// views a chunk, its size checked. Device memory is released on the stream
+// it was allocated on, so a chunk allocated on a stream must be destroyed
+// before that stream is. Errors are aether::Error in the
 // "<op> failed on <where>, size=<n> bytes (<detail>)" form.
 #pragma once
 

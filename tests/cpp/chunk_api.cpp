@@ -81,14 +81,12 @@ void hostCases() {
 #if defined(__CUDACC__)
 namespace {
 
-void deviceCases() {
+void deviceChunks(cudaStream_t st) {
     const std::size_t n = 1 << 20;
     aether::Chunk pin = aether::Chunk::allocate(kPinned, n * sizeof(double));
     aether::Chunk back = aether::Chunk::allocate(kPinned, n * sizeof(double));
     auto* p = reinterpret_cast<double*>(pin.data());
     for (std::size_t k = 0; k < n; ++k) p[k] = double(k) * 0.5;
-    cudaStream_t st = nullptr;
-    AETHER_CHECK_CUDA(cudaStreamCreate(&st));
     aether::Chunk dev = aether::Chunk::allocate(kDev, n * sizeof(double), st);
     CHECK(dev.streamOrdered() && dev.stream() == st && dev.owns());
     aether::copyAsync(dev, pin, st);   // page-locked -> device
@@ -111,6 +109,13 @@ void deviceCases() {
     // a device view over a chunk, used by the engine's runtime evaluation
     auto dv = aether::make_view<double, 2, aether::dyn>(dev, n / 2);
     CHECK(dv.device() == kDev && dv.data() == reinterpret_cast<double*>(dev.data()));
+    AETHER_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+void deviceCases() {
+    cudaStream_t st = nullptr;
+    AETHER_CHECK_CUDA(cudaStreamCreate(&st));
+    deviceChunks(st);   // every chunk is gone before its stream is destroyed
     AETHER_CHECK_CUDA(cudaStreamDestroy(st));
 }
 
