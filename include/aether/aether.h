@@ -39,6 +39,7 @@
 #include "aether/eval.h"
 #include "aether/accum.h"
 #include "aether/accum_run.h"
+#include "aether/accum_atomic.h"
 #include "aether/rt.h"
 #include "aether/batch.h"
 #include "aether/device_flag.h"
